@@ -1,0 +1,432 @@
+"""Benchmark: GTEPS and HBM-roofline fraction of the five push algorithms on R-MAT scale 22.
+
+Workload (one "step" = one pass of the hot path over the graph, every algorithm once):
+  R-MAT scale 22 (4,194,304 vertices), edge factor 16 (67,108,864 edges), a/b/c/d = .57/.19/.19/.05,
+  seed 1, uint32 weights uniform in [1,63], Tigr K = 8 (--k 4|8|16).
+    BFS, SSSP, SSWP  sync_push_dd from the highest-out-degree vertex
+    CC               async_push_dd (every vertex seeded) on the symmetrised arc set (134M arcs)
+    PageRank         sync_push_td (Jacobi pull), d = 0.85, stop at ||x-x*||_1/||x||_1 <= 1e-7
+  value = sum over the step of TEPS edges (m_r per traversal, m for CC, sweeps*m for PageRank)
+          / device time of the step (CUDA events on the launching stream), whole job over all ranks.
+  e2e   = the same metric through the C ABI with host buffers: pinned host edge lists copied in,
+          virtual graphs built on the GPU, results copied back to host, every step.
+Inputs are larger than L2 (the part arrays are ~0.7 GB) and L2 is also flushed (256 MB write)
+between timed steps.
+
+--impl reference: the reference's CPU path (its seq_cpu sweeps -- oracle/_ref when built on this
+machine, else the oracle's C restatement of it; PageRank: the FP64 oracle, the reference has none) on
+a bounded sample (R-MAT scale 18, same parameters), all host threads, same metric and unit.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SCALE, EF, SEED = 22, 16, 1
+SAMPLE_SCALE = 18
+ALGO_PLAN = [("bfs", "sync_push_dd"), ("sssp", "sync_push_dd"), ("sswp", "sync_push_dd"),
+             ("cc", "async_push_dd"), ("pr", "sync_push_td")]
+PR_TOL = 1e-7
+
+
+def workload_name(scale: int, K: int) -> str:
+    return (f"R-MAT s{scale} ef{EF} a/b/c/d=.57/.19/.19/.05 seed {SEED} w~U[1,63]; BFS/SSSP/SSWP sync_push_dd "
+            f"from max-out-degree vertex, CC async_push_dd on the symmetrised graph, PR sync_push_td d=0.85 "
+            f"tol 1e-7; K={K}")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def load_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    try:
+        t = json.loads(p.read_text())
+        e = t.get(workload, {}).get(kernel)
+        return None if e is None else float(e["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        cmd = ["nvidia-smi", "-i", str(self.device),
+               "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def make_inputs(E, scale: int):
+    s, d, w = E.gen_rmat(scale, EF, seed=SEED, wmin=1, wmax=63)
+    ss, ds, ws = E.symmetrize(s, d, w)
+    n = 1 << scale
+    return n, (s, d, w), (ss, ds, ws)
+
+
+def teps_edges(algo: str, res: dict, m: int, m_sym: int) -> float:
+    if algo == "pr":
+        return float(res["iterations"]) * m
+    if algo == "cc":
+        return float(m_sym)
+    return float(res["reached_edges"])
+
+
+def run_step(vg, vg_sym, source, outs, stream, results):
+    for algo, variant in ALGO_PLAN:
+        g = vg_sym if algo == "cc" else vg
+        _, res = g.run(algo, variant, source, out_device_ptr=outs[algo], stream=stream,
+                       pr_tolerance=PR_TOL)
+        results[algo] = res
+
+
+def bench_gpu(args) -> None:
+    import torch
+
+    import eegraph_gb300 as E
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    E.lib().eeg_set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    scale = args.scale
+    n, (s, d, w), (ss, ds, ws) = make_inputs(E, scale)
+    m, m_sym = s.size, ss.size
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    vg = E.VirtualGraph.build(n, s, d, w, K=args.k, reverse=True, stream=stream)
+    vg_sym = E.VirtualGraph.build(n, ss, ds, ws, K=args.k, stream=stream)
+    info = vg.info()
+    source = info["max_degree_vertex"]
+    outs_t = {a: torch.empty(n, dtype=torch.int32, device=dev) for a, _ in ALGO_PLAN}
+    outs = {a: t.data_ptr() for a, t in outs_t.items()}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    results: dict = {}
+    for _ in range(args.warmup):
+        run_step(vg, vg_sym, source, outs, stream, results)
+    torch.cuda.synchronize()
+
+    per_algo = {a: {"ms": [], "edges": [], "bytes": [], "iters": []} for a, _ in ALGO_PLAN}
+    step_ms = []
+    launches = 0
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(float(i))  # L2 flush between timed steps (outside the events)
+            starts[i].record()
+            run_step(vg, vg_sym, source, outs, stream, results)
+            ends[i].record()
+            for a, _ in ALGO_PLAN:
+                r = results[a]
+                per_algo[a]["ms"].append(r["kernel_ms"])
+                per_algo[a]["edges"].append(teps_edges(a, r, m, m_sym))
+                per_algo[a]["bytes"].append(r["algorithmic_bytes"])
+                per_algo[a]["iters"].append(r["iterations"])
+                launches += r["launches"]
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    step_ms = [starts[i].elapsed_time(ends[i]) for i in range(args.steps)]
+    total_ms = sum(step_ms)
+    step_edges = sum(per_algo[a]["edges"][-1] for a, _ in ALGO_PLAN)
+    total_edges = step_edges * args.steps
+    if world > 1:
+        t = torch.tensor([total_ms, total_edges], dtype=torch.float64, device=dev)
+        mx = t.clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm_ = t.clone()
+        torch.distributed.all_reduce(sm_, op=torch.distributed.ReduceOp.SUM)
+        total_ms_all, total_edges_all = float(mx[0]), float(sm_[1])
+    else:
+        total_ms_all, total_edges_all = total_ms, total_edges
+    value = total_edges_all / (total_ms_all * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers (timed on the host around the whole step)
+    import torch as _t
+
+    pin = {k: _t.from_numpy(v).pin_memory().numpy() for k, v in
+           {"s": s, "d": d, "w": w, "ss": ss, "ds": ds, "ws": ws}.items()}
+    host_out = {a: np.empty(n, np.float32 if a == "pr" else np.uint32) for a, _ in ALGO_PLAN}
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g1 = E.VirtualGraph.build(n, pin["s"], pin["d"], pin["w"], K=args.k, reverse=True, stream=stream)
+        g2 = E.VirtualGraph.build(n, pin["ss"], pin["ds"], pin["ws"], K=args.k, stream=stream)
+        src_e2e = g1.info()["max_degree_vertex"]
+        for algo, variant in ALGO_PLAN:
+            (g2 if algo == "cc" else g1).run(algo, variant, src_e2e, out=host_out[algo], stream=stream,
+                                             pr_tolerance=PR_TOL)
+        g1.close()
+        g2.close()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total_ms = sum(e2e_ms)
+    if world > 1:
+        tt = torch.tensor([e2e_total_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_total_ms = float(tt[0])
+    e2e_value = total_edges_all / (e2e_total_ms * 1e-3) / 1e9
+    h2d = 4 * (3 * m + 3 * m_sym)
+    d2h = 4 * n * len(ALGO_PLAN)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+
+    peak, peak_kind = load_peaks()
+    algo_summary = {}
+    for a, _ in ALGO_PLAN:
+        ms = statistics.median(per_algo[a]["ms"])
+        by = statistics.median(per_algo[a]["bytes"])
+        ed = statistics.median(per_algo[a]["edges"])
+        algo_summary[a] = {"kernel_ms": round(ms, 4), "gteps": round(ed / (ms * 1e-3) / 1e9, 3),
+                           "iterations": int(statistics.median(per_algo[a]["iters"])),
+                           "algorithmic_GB": round(by / 1e9, 4),
+                           "achieved_GBs": round(by / (ms * 1e-3) / 1e9, 1),
+                           "roofline_frac": round(by / (ms * 1e-3) / 1e9 / peak, 4)}
+    dom = max(algo_summary, key=lambda a: algo_summary[a]["kernel_ms"])
+    kern_name = {"bfs": "k_traverse<OP_BFS>", "sssp": "k_traverse<OP_SSSP>", "sswp": "k_traverse<OP_SSWP>",
+                 "cc": "k_traverse<OP_CC>", "pr": "k_pagerank"}[dom]
+    wl = workload_name(scale, args.k)
+    ach = algo_summary[dom]["achieved_GBs"]
+    line = {
+        "metric": "GTEPS (sum over BFS,SSSP,SSWP,CC,PR of TEPS edges / device time)",
+        "value": round(value, 3),
+        "unit": "GTEPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total_ms_all / args.steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32 (BFS/SSSP/SSWP/CC), f32 (PageRank)",
+        "data": "synthetic (seeded R-MAT, generated in-process)",
+        "config": {"workload": wl, "scale": scale, "edge_factor": EF, "K": args.k, "vertices": n, "edges": m,
+                   "cc_arcs": m_sym, "source": source, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (part arrays ~0.7 GB) and 256 MB L2 flush between timed steps"},
+        "per_algo": algo_summary,
+        "roofline": {"bound": "hbm", "kernel": kern_name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                     "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                     "traffic": load_traffic(kern_name, f"s{scale}_k{args.k}")},
+        "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(e2e_total_ms / args.steps, 3)},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(threads=1, budget_s=args.cpu_budget)
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------- CPU (reference) path
+def cpu_jobs(E, scale):
+    n, (s, d, w), (ss, ds, ws) = make_inputs(E, scale)
+    deg = np.bincount(s, minlength=n)
+    order = np.argsort(-deg, kind="stable")
+    return n, (s, d, w), (ss, ds, ws), order
+
+
+def cpu_run(job, n, g, gsym, use_ref):
+    """One CPU job; returns (TEPS edges, seconds of the algorithm alone)."""
+    import oracle
+
+    algo, source = job
+    s, d, w = g
+    if algo == "pr":
+        t0 = time.perf_counter()
+        x, it = oracle.pagerank(n, s, d, 0.85, 1e-7 * 0.15 / 0.85)
+        return float(it) * s.size, time.perf_counter() - t0
+    if algo == "cc":
+        s, d, w = gsym
+    if use_ref:
+        out, secs = oracle.ref_seq_cpu(algo, n, s, d, w, source, timed=True)
+    else:
+        out, _, secs = oracle.seq_sweep(algo, n, s, d, w, source, timed=True)
+    if algo == "cc":
+        return float(s.size), secs
+    reached = (out != 0) if algo == "sswp" else (out != 4294967294)
+    return float(np.bincount(s, minlength=n)[reached].sum()), secs
+
+
+def cpu_baseline(threads: int, budget_s: float, scale: int = SAMPLE_SCALE) -> dict:
+    """The reference's CPU path on a bounded sample: one pass of the five algorithms."""
+    import eegraph_gb300 as E
+    import oracle
+
+    use_ref = oracle.ref_available()
+    n, g, gsym, order = cpu_jobs(E, scale)
+    jobs = [("bfs", int(order[0])), ("sssp", int(order[0])), ("sswp", int(order[0])), ("cc", 0), ("pr", 0)]
+    tot_e, tot_t = 0.0, 0.0
+    t_start = time.perf_counter()
+    for j in jobs:
+        e, t = cpu_run(j, n, g, gsym, use_ref)
+        tot_e += e
+        tot_t += t
+        if time.perf_counter() - t_start > budget_s:
+            break
+    return {"value": round(tot_e / tot_t / 1e9, 5), "unit": "GTEPS", "cores": threads,
+            "kind": "reference" if use_ref else "port",
+            "sample": f"R-MAT s{scale} ef{EF} (same a/b/c/d, seed, weights): BFS/SSSP/SSWP/CC via the reference's "
+                      f"seq_cpu sweeps ({'oracle/_ref' if use_ref else 'oracle C restatement'}), PR via the FP64 oracle"}
+
+
+def bench_reference(args) -> None:
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import concurrent.futures as cf
+
+    import eegraph_gb300 as E
+    import oracle
+
+    use_ref = oracle.ref_available()
+    threads = args.cpu_threads or os.cpu_count() or 1
+    n, g, gsym, order = cpu_jobs(E, SAMPLE_SCALE)
+    # one step = T concurrent independent jobs (all host threads): traversals from different sources, CC, PR
+    base = [("cc", 0), ("pr", 0)]
+    trav = [(a, int(order[i % 64])) for i in range(max(threads - 2, 3)) for a in ("bfs", "sssp", "sswp")][: max(threads - 2, 3)]
+    jobs = base + trav
+
+    def step():
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            res = list(ex.map(lambda j: cpu_run(j, n, g, gsym, use_ref), jobs))
+        return sum(e for e, _ in res), time.perf_counter() - t0
+
+    for _ in range(args.warmup):
+        step()
+    tot_e, tot_t = 0.0, 0.0
+    for _ in range(args.steps):
+        e, t = step()
+        tot_e += e
+        tot_t += t
+    value = tot_e / tot_t / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "GTEPS (sum over BFS,SSSP,SSWP,CC,PR of TEPS edges / device time)",
+        "value": round(value, 5), "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(tot_t / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 (BFS/SSSP/SSWP/CC), f64 (PageRank oracle)",
+        "data": "synthetic (seeded R-MAT)",
+        "config": {"workload": workload_name(SCALE, 8), "sample_scale": SAMPLE_SCALE, "threads": threads},
+        "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": threads,
+                         "kind": "reference" if use_ref else "port",
+                         "sample": f"per step {len(jobs)} concurrent jobs on R-MAT s{SAMPLE_SCALE} ef{EF}: "
+                                   "BFS/SSSP/SSWP seq_cpu from the top-degree vertices, CC seq_cpu, FP64 PageRank"},
+        "e2e": {"value": round(value, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--k", type=int, default=8, choices=[4, 8, 16])
+    ap.add_argument("--scale", type=int, default=SCALE)
+    ap.add_argument("--cpu-budget", type=float, default=30.0)
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

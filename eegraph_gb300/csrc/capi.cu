@@ -1,0 +1,380 @@
+// capi.cu -- implementation of the C ABI declared in include/eegraph_c.h.
+//
+// Replaces the library entry points eegraph_<algo>[_um] (reference include/eegraph.cuh:21-39,
+// src/eegraph.cu) at the C level: handles own their device memory, results go to caller-owned
+// buffers, every failure is a returned status (the reference calls exit(), include/gpu_error_check.cuh:8-16).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace eeg {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+eeg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    g_last_error = buf;
+    if (e == cudaErrorMemoryAllocation) return EEG_ERR_NOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return EEG_ERR_NO_DEVICE;
+    return EEG_ERR_CUDA;
+}
+
+eeg_status vg_alloc(eeg_vgraph* vg, void** p, size_t bytes) {
+    if (bytes == 0) bytes = 4;
+    cudaError_t e;
+    if (vg->managed) {
+        e = cudaMallocManaged(p, bytes);
+        if (e == cudaSuccess) {
+            cudaMemLocation loc{};
+            loc.type = cudaMemLocationTypeDevice;
+            loc.id = vg->device;
+            cudaMemAdvise(*p, bytes, cudaMemAdviseSetPreferredLocation, loc);
+            (void)cudaGetLastError();
+        }
+    } else {
+        e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, vg->managed ? "cudaMallocManaged" : "cudaMalloc", __FILE__, __LINE__);
+    }
+    return EEG_OK;
+}
+
+void vg_free(eeg_vgraph*, void* p) {
+    if (p) cudaFree(p);
+}
+
+static void free_dir(eeg_vgraph* vg, VDir& d) {
+    vg_free(vg, d.vstart);
+    vg_free(vg, d.vowner);
+    vg_free(vg, d.vcol);
+    vg_free(vg, d.vw);
+    vg_free(vg, d.deg);
+    d = VDir{};
+}
+
+static void free_ws(eeg_vgraph* vg) {
+    Workspace& w = vg->ws;
+    vg_free(vg, w.dist);
+    vg_free(vg, w.q[0]);
+    vg_free(vg, w.q[1]);
+    vg_free(vg, w.stamp);
+    if (w.activity) cudaFree(w.activity);
+    if (w.tctrl) cudaFree(w.tctrl);
+    vg_free(vg, w.x);
+    vg_free(vg, w.contrib[0]);
+    vg_free(vg, w.contrib[1]);
+    vg_free(vg, w.acc);
+    vg_free(vg, w.cross);
+    if (w.pctrl) cudaFree(w.pctrl);
+    if (w.stats) cudaFree(w.stats);
+    if (w.ev[0]) cudaEventDestroy(w.ev[0]);
+    if (w.ev[1]) cudaEventDestroy(w.ev[1]);
+    w = Workspace{};
+}
+
+}  // namespace eeg
+
+using namespace eeg;
+
+extern "C" {
+
+EEG_API const char* eeg_status_string(eeg_status s) {
+    switch (s) {
+        case EEG_OK: return "ok";
+        case EEG_ERR_INVALID: return "invalid argument";
+        case EEG_ERR_IO: return "i/o error";
+        case EEG_ERR_CUDA: return "CUDA error";
+        case EEG_ERR_NOMEM: return "out of memory";
+        case EEG_ERR_TIMEOUT: return "device wait timed out";
+        case EEG_ERR_ITER_CAP: return "iteration cap reached";
+        case EEG_ERR_UNSUPPORTED: return "unsupported";
+        case EEG_ERR_NO_DEVICE: return "no CUDA device";
+        case EEG_ERR_ENERGY: return "energy unavailable";
+    }
+    return "unknown status";
+}
+
+EEG_API const char* eeg_last_error(void) { return g_last_error.c_str(); }
+
+EEG_API const char* eeg_version(void) { return "eegraph-gb300 0.1 (sm_103a)"; }
+
+EEG_API int eeg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+EEG_API eeg_status eeg_set_device(int device) {
+    EEG_CUDA(cudaSetDevice(device));
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_managed_alloc(size_t bytes, void** out) {
+    if (!out) {
+        set_last_error("null output pointer");
+        return EEG_ERR_INVALID;
+    }
+    *out = nullptr;
+    EEG_CUDA(cudaMallocManaged(out, bytes ? bytes : 4));
+    return EEG_OK;
+}
+
+EEG_API void eeg_managed_free(void* p) {
+    if (p) cudaFree(p);
+}
+
+EEG_API void eeg_options_init(eeg_options* o) {
+    if (o) memset(o, 0, sizeof(*o));
+}
+
+static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                             uint32_t K, uint32_t flags, void* stream, eeg_vgraph** out) {
+    if (!out) {
+        set_last_error("null output handle");
+        return EEG_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (K != 4 && K != 8 && K != 16) {
+        set_last_error("K must be 4, 8 or 16");
+        return EEG_ERR_UNSUPPORTED;
+    }
+    if (m && (!src || !dst)) {
+        set_last_error("null edge arrays");
+        return EEG_ERR_INVALID;
+    }
+    if (m >= 0xFFFFFFFFull || n == 0xFFFFFFFFu) {
+        set_last_error("graph too large for 32-bit ids/offsets");
+        return EEG_ERR_UNSUPPORTED;
+    }
+    if (eeg_device_count() == 0) {
+        set_last_error("no CUDA device visible");
+        return EEG_ERR_NO_DEVICE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    eeg_vgraph* vg = new eeg_vgraph();
+    cudaGetDevice(&vg->device);
+    vg->n = n;
+    vg->m = m;
+    vg->K = K;
+    vg->flags = flags;
+    vg->managed = (flags & EEG_VG_MANAGED) != 0;
+    vg->weighted = true;
+
+    auto fail = [&](eeg_status s) {
+        eeg_vgraph_destroy(vg);
+        return s;
+    };
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        set_last_error("cudaEventCreate failed");
+        delete vg;
+        return EEG_ERR_CUDA;
+    }
+    const bool on_device = (flags & EEG_VG_INPUT_DEVICE) != 0;
+    const uint32_t *ds = src, *dd = dst, *dw = w;
+    uint32_t* tmp = nullptr;
+    eeg_status s = EEG_OK;
+    cudaEventRecord(e0, st);
+    if (!on_device && m > 0) {
+        const size_t words = (size_t)m * (w ? 3 : 2);
+        cudaError_t ce = cudaMallocAsync((void**)&tmp, words * sizeof(uint32_t), st);
+        if (ce != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return fail(cuda_fail(ce, "cudaMallocAsync(edges)", __FILE__, __LINE__));
+        }
+        cudaMemcpyAsync(tmp, src, m * 4, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(tmp + m, dst, m * 4, cudaMemcpyHostToDevice, st);
+        if (w) cudaMemcpyAsync(tmp + 2 * m, w, m * 4, cudaMemcpyHostToDevice, st);
+        ds = tmp;
+        dd = tmp + m;
+        dw = w ? tmp + 2 * m : nullptr;
+    }
+    s = build_direction(vg, &vg->fwd, ds, dd, dw, false, st);
+    if (s == EEG_OK && (flags & EEG_VG_REVERSE)) {
+        s = build_direction(vg, &vg->rev, ds, dd, nullptr, true, st);
+        vg->has_rev = (s == EEG_OK);
+    }
+    if (tmp) cudaFreeAsync(tmp, st);
+    cudaEventRecord(e1, st);
+    cudaError_t ce = cudaStreamSynchronize(st);
+    if (s == EEG_OK && ce != cudaSuccess) s = cuda_fail(ce, "virtual graph build", __FILE__, __LINE__);
+    if (s == EEG_OK) cudaEventElapsedTime(&vg->build_ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (s != EEG_OK) return fail(s);
+    *out = vg;
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_vgraph_build(const eeg_graph* g, uint32_t K, uint32_t flags, void* stream, eeg_vgraph** out) {
+    if (!g) {
+        set_last_error("null graph");
+        return EEG_ERR_INVALID;
+    }
+    // 1-based files are shifted down by one, as VirtualGraph::VirtualGraph does (src/virtual_graph.cpp:5-12)
+    uint32_t f = flags & ~(uint32_t)EEG_VG_INPUT_DEVICE;
+    if (!g->has_zero_id) f |= EEG_VG_SHIFT_ONE;
+    else f &= ~(uint32_t)EEG_VG_SHIFT_ONE;
+    return build_impl(g->num_nodes, g->num_edges, g->src.data(), g->dst.data(),
+                      g->weight.empty() ? nullptr : g->weight.data(), K, f, stream, out);
+}
+
+EEG_API eeg_status eeg_vgraph_build_arrays(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src,
+                                           const uint32_t* dst, const uint32_t* weight, uint32_t K, uint32_t flags,
+                                           void* stream, eeg_vgraph** out) {
+    return build_impl(num_nodes, num_edges, src, dst, weight, K, flags, stream, out);
+}
+
+EEG_API eeg_status eeg_vgraph_get_info(const eeg_vgraph* vg, eeg_vgraph_info* o) {
+    if (!vg || !o) {
+        set_last_error("null argument");
+        return EEG_ERR_INVALID;
+    }
+    o->num_nodes = vg->n;
+    o->num_edges = vg->m;
+    o->K = vg->K;
+    o->num_parts = vg->fwd.P;
+    o->num_rparts = vg->has_rev ? vg->rev.P : 0;
+    o->max_out_degree = vg->max_deg;
+    o->max_degree_vertex = vg->max_deg_vertex;
+    o->device_bytes = vg->bytes;
+    o->build_ms = vg->build_ms;
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_vgraph_download(const eeg_vgraph* vg, uint32_t* vstart, uint32_t* vowner, uint32_t* vcol,
+                                       uint32_t* vw, uint32_t* outdeg) {
+    if (!vg) {
+        set_last_error("null argument");
+        return EEG_ERR_INVALID;
+    }
+    EEG_CUDA(cudaSetDevice(vg->device));
+    const size_t n = vg->n, P = vg->fwd.P, S = P * vg->K;
+    if (vstart) EEG_CUDA(cudaMemcpy(vstart, vg->fwd.vstart, 4 * (n + 1), cudaMemcpyDeviceToHost));
+    if (vowner && P) EEG_CUDA(cudaMemcpy(vowner, vg->fwd.vowner, 4 * P, cudaMemcpyDeviceToHost));
+    if (vcol && S) EEG_CUDA(cudaMemcpy(vcol, vg->fwd.vcol, 4 * S, cudaMemcpyDeviceToHost));
+    if (vw && S && vg->fwd.vw) EEG_CUDA(cudaMemcpy(vw, vg->fwd.vw, 4 * S, cudaMemcpyDeviceToHost));
+    if (outdeg) EEG_CUDA(cudaMemcpy(outdeg, vg->fwd.deg, 4 * n, cudaMemcpyDeviceToHost));
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_vgraph_export_reference_layout(const eeg_vgraph* vg, uint32_t* nodePointer,
+                                                      uint32_t* edgeList, uint32_t* partNodePointer) {
+    if (!vg) {
+        set_last_error("null argument");
+        return EEG_ERR_INVALID;
+    }
+    const size_t n = vg->n, P = vg->fwd.P, K = vg->K;
+    std::vector<uint32_t> vstart(n + 1), deg(n), vcol(P * K), vw(P * K, 1u);
+    EEG_TRY(eeg_vgraph_download(vg, vstart.data(), nullptr, vcol.data(), vg->fwd.vw ? vw.data() : nullptr, deg.data()));
+    uint64_t counter = 0, part = 0;
+    for (size_t v = 0; v < n; ++v) {
+        if (nodePointer) nodePointer[v] = (uint32_t)counter;
+        if (edgeList) {
+            edgeList[counter] = deg[v];
+            const size_t base = (size_t)vstart[v] * K;
+            for (uint32_t r = 0; r < deg[v]; ++r) {
+                edgeList[counter + 1 + 2 * (uint64_t)r] = vcol[base + r];
+                edgeList[counter + 2 + 2 * (uint64_t)r] = vw[base + r];
+            }
+        }
+        counter += 2 * (uint64_t)deg[v] + 1;
+        const uint32_t np = vstart[v + 1] - vstart[v];
+        for (uint32_t j = 0; j < np; ++j, ++part) {
+            if (partNodePointer) {
+                partNodePointer[2 * part] = (uint32_t)v;
+                partNodePointer[2 * part + 1] = j;
+            }
+        }
+    }
+    return EEG_OK;
+}
+
+EEG_API void eeg_vgraph_destroy(eeg_vgraph* vg) {
+    if (!vg) return;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(vg->device);
+    free_dir(vg, vg->fwd);
+    free_dir(vg, vg->rev);
+    free_ws(vg);
+    cudaSetDevice(prev);
+    delete vg;
+}
+
+EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, uint32_t source,
+                           const eeg_options* opts, void* out, int out_on_device, uint32_t* activity,
+                           uint32_t activity_cap, void* stream, eeg_result* res) {
+    if (!vg) {
+        set_last_error("null graph handle");
+        return EEG_ERR_INVALID;
+    }
+    if ((unsigned)variant > 3u) {
+        set_last_error("unknown variant");
+        return EEG_ERR_INVALID;
+    }
+    eeg_options o;
+    eeg_options_init(&o);
+    if (opts) o = *opts;
+    eeg_result r;
+    memset(&r, 0, sizeof(r));
+    cudaStream_t st = (cudaStream_t)stream;
+    EEG_CUDA(cudaSetDevice(vg->device));
+    eeg_status s;
+    if (algo == EEG_PR) {
+        s = run_pagerank(vg, variant, o, st, &r);
+        if (s == EEG_OK || s == EEG_ERR_ITER_CAP) {
+            if (out) {
+                EEG_CUDA(cudaMemcpyAsync(out, vg->ws.x, sizeof(float) * vg->n,
+                                         out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+                EEG_CUDA(cudaStreamSynchronize(st));
+            }
+            r.reached_vertices = vg->n;
+            r.reached_edges = vg->m;
+            r.algorithmic_bytes = (double)r.iterations * (12.0 * vg->n + 8.0 * (double)vg->m);
+            r.gteps = r.kernel_ms > 0 ? (double)r.iterations * (double)vg->m / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
+        }
+        if (activity && activity_cap && res) r.num_activity = 0;
+    } else {
+        int op;
+        switch (algo) {
+            case EEG_BFS: op = OP_BFS; break;
+            case EEG_SSSP: op = OP_SSSP; break;
+            case EEG_SSWP: op = OP_SSWP; break;
+            case EEG_CC: op = OP_CC; break;
+            default: set_last_error("unknown algorithm"); return EEG_ERR_INVALID;
+        }
+        s = run_traversal(vg, op, variant, source, o, st, &r, activity, activity_cap);
+        if (s == EEG_OK || s == EEG_ERR_ITER_CAP) {
+            if (out) {
+                EEG_CUDA(cudaMemcpyAsync(out, vg->ws.dist, sizeof(uint32_t) * vg->n,
+                                         out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+            }
+            uint64_t nr = 0, mr = 0;
+            eeg_status s2 = reached_stats(vg, op, vg->ws.dist, st, &nr, &mr);
+            if (s2 != EEG_OK) return s2;
+            r.reached_vertices = nr;
+            r.reached_edges = mr;
+            r.algorithmic_bytes = 12.0 * (double)nr + (op == OP_BFS ? 8.0 : 12.0) * (double)mr;
+            r.gteps = r.kernel_ms > 0 ? (double)mr / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
+            r.launches = 2;  // persistent traversal kernel + reached-set statistics
+        }
+    }
+    if (res) *res = r;
+    return s;
+}
+
+}  // extern "C"

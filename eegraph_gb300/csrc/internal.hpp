@@ -1,0 +1,112 @@
+// internal.hpp -- handle layouts shared by the C ABI implementation and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+// Host edge list (the reference's Graph: src/graph.cpp, include/graph.hpp:28-50).
+struct eeg_graph {
+    uint32_t num_nodes = 0;
+    uint64_t num_edges = 0;
+    bool has_zero_id = false;
+    bool is_weighted = false;
+    std::vector<uint32_t> src, dst, weight;
+};
+
+namespace eeg {
+
+// One K-bounded virtual graph (forward, or transposed for pull kernels) in HBM.
+struct VDir {
+    uint64_t P = 0;               // number of parts
+    uint32_t* vstart = nullptr;   // n+1: first part of each vertex
+    uint32_t* vowner = nullptr;   // P: owning vertex of each part
+    uint32_t* vcol = nullptr;     // P*K: neighbour ids (NO_EDGE padding)
+    uint32_t* vw = nullptr;       // P*K: weights (uint32; float bits for PageRank weights) or null
+    uint32_t* deg = nullptr;      // n: degree in this direction
+};
+
+// Control block of the traversal kernel (device memory).
+struct TravCtrl {
+    BarrierWords bw;
+    uint32_t qparts[3];   // parts enqueued per round (rotating; TD: improvement flag)
+    uint32_t qverts[3];   // vertices enqueued per round (rotating)
+    uint32_t iterations;
+    uint32_t pad;
+    unsigned long long parts_processed;
+    unsigned long long edges_scanned;
+    unsigned long long updates;
+};
+
+// Control block of the PageRank kernels.
+struct PRCtrl {
+    BarrierWords bw;
+    double resid[3];     // ||x_{k+1}-x_k||_1 per sweep (rotating)
+    double norm[3];      // ||x_{k+1}||_1 per sweep (rotating)
+    uint32_t iterations;
+    uint32_t pad;
+    double last_resid;
+    double last_norm;
+    unsigned long long edges_scanned;
+};
+
+struct Workspace {
+    // traversal
+    uint32_t* dist = nullptr;     // n
+    uint32_t* q[2] = {nullptr, nullptr};  // P each
+    uint32_t* stamp = nullptr;    // n
+    uint32_t* activity = nullptr; // device copy of the activity vector
+    uint32_t activity_cap = 0;
+    TravCtrl* tctrl = nullptr;
+    // PageRank
+    float* x = nullptr;           // n
+    float* contrib[2] = {nullptr, nullptr};  // n each
+    double* acc = nullptr;        // n (partials of vertices whose parts cross warp chunks)
+    uint32_t* cross = nullptr;    // list of those vertices
+    uint32_t ncross = 0;
+    unsigned long long zero_in = 0;  // vertices with no in-edges
+    double zero_in_norm = 0.0;    // their constant share of ||x||_1
+    PRCtrl* pctrl = nullptr;
+    // misc
+    unsigned long long* stats = nullptr;  // reached counters
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+}  // namespace eeg
+
+struct eeg_vgraph {
+    int device = 0;
+    uint32_t n = 0;
+    uint64_t m = 0;
+    uint32_t K = 8;
+    uint32_t flags = 0;
+    bool managed = false;
+    eeg::VDir fwd, rev;
+    bool has_rev = false;
+    bool weighted = true;
+    uint32_t max_deg = 0, max_deg_vertex = 0;
+    uint64_t bytes = 0;
+    float build_ms = 0.f;
+    eeg::Workspace ws;
+};
+
+namespace eeg {
+
+// allocation helpers (device or managed per graph)
+eeg_status vg_alloc(eeg_vgraph* vg, void** p, size_t bytes);
+void vg_free(eeg_vgraph* vg, void* p);
+
+// builder (builder.cu)
+eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst,
+                           const uint32_t* d_w, bool reverse, cudaStream_t st);
+
+// kernels (traverse.cu / pagerank.cu)
+eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t source, const eeg_options& o,
+                         cudaStream_t st, eeg_result* res, uint32_t* activity_host, uint32_t activity_cap);
+eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& o, cudaStream_t st, eeg_result* res);
+eeg_status reached_stats(eeg_vgraph* vg, int op, const uint32_t* d_dist, cudaStream_t st, uint64_t* n_r, uint64_t* m_r);
+
+}  // namespace eeg

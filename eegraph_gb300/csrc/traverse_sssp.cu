@@ -1,0 +1,12 @@
+// traverse_sssp.cu -- instantiation of the persistent push kernels for SSSP (templates in traverse.cuh).
+#include "traverse.cuh"
+
+namespace eeg {
+namespace trav {
+
+eeg_status launch_sssp(const TravArgs& args, bool td, uint32_t K, int device, uint32_t bps, cudaStream_t st) {
+    return td ? launch_k<OP_SSSP, true>(args, K, device, bps, st) : launch_k<OP_SSSP, false>(args, K, device, bps, st);
+}
+
+}  // namespace trav
+}  // namespace eeg

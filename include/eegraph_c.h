@@ -1,0 +1,250 @@
+/*
+ * eegraph_c.h -- C ABI of the GB300-native EEGraph push-kernel library.
+ *
+ * Every entry point takes plain pointers and sizes, returns an eeg_status and never calls exit().
+ * The C++ facade (include/eegraph.hpp) and the per-algorithm executables are built on top of it.
+ *
+ * Reference interfaces each group replaces (paths inside rwatling/EEGraph):
+ *   loader            Graph::Graph / Graph::ReadGraph              src/graph.cpp:3-113, include/graph.hpp:28-50
+ *   virtual graph     VirtualGraph::VirtualGraph / MakeGraph       src/virtual_graph.cpp:3-112, include/virtual_graph.hpp:8-26
+ *                     UMVirtualGraph (managed-memory twin)          src/um_virtual_graph.cu:36-111
+ *   runs              eegraph_{bfs,sssp,sswp,cc,pr}[_um]            include/eegraph.cuh:21-39, src/eegraph.cu
+ *                     (+ the host do/while loop around the kernels src/eegraph.cu:89-211)
+ *   kernels           {bfs,sssp,sswp,cc,pr}::{sync,async}_push_{td,dd} src/{bfs,sssp,sswp,cc,pr}.cu
+ *                     clearLabel/mixLabels/moveUpLabels/sumLabels   src/gpu_utils.cu:3-34 (fused)
+ *   energy            nvmlClass                                     include/nvmlClass.cuh:77-356
+ *   errors            gpuErrorcheck -> exit(code)                   include/gpu_error_check.cuh:8-16
+ */
+#ifndef EEGRAPH_C_H
+#define EEGRAPH_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define EEG_API __attribute__((visibility("default")))
+#else
+#define EEG_API
+#endif
+
+/* ------------------------------------------------------------------ status / enums */
+
+typedef enum eeg_status {
+    EEG_OK = 0,
+    EEG_ERR_INVALID = 1,      /* bad argument (null pointer, source out of range, unknown algo ...) */
+    EEG_ERR_IO = 2,           /* file missing / unreadable / unrecognised extension                 */
+    EEG_ERR_CUDA = 3,         /* a CUDA runtime call failed (message in eeg_last_error())            */
+    EEG_ERR_NOMEM = 4,        /* device or host allocation failed                                    */
+    EEG_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (grid barrier)                   */
+    EEG_ERR_ITER_CAP = 6,     /* the iteration cap was reached before the fixed point                */
+    EEG_ERR_UNSUPPORTED = 7,  /* combination not available (e.g. K not in {4,8,16})                  */
+    EEG_ERR_NO_DEVICE = 8,    /* no CUDA device visible                                              */
+    EEG_ERR_ENERGY = 9        /* NVML could not be started: energy unavailable                       */
+} eeg_status;
+
+/* Algorithms of the reference (one executable / eegraph_<algo> each). */
+typedef enum eeg_algo {
+    EEG_BFS = 0,
+    EEG_SSSP = 1,
+    EEG_SSWP = 2,
+    EEG_CC = 3,  /* the reference's min-plus label propagation: label(v)=min(v, min_u label(u)+w(u,v)) */
+    EEG_PR = 4
+} eeg_algo;
+
+/* Same numbering as the reference's `enum Variant` (include/globals.hpp:36-41). */
+typedef enum eeg_variant {
+    EEG_ASYNC_PUSH_TD = 0,
+    EEG_ASYNC_PUSH_DD = 1,
+    EEG_SYNC_PUSH_TD = 2,
+    EEG_SYNC_PUSH_DD = 3
+} eeg_variant;
+
+/* Reference constants (include/globals.hpp:30-32). */
+#define EEG_DIST_INFINITY 4294967294u /* UINT_MAX - 1 */
+#define EEG_DEFAULT_K 8u              /* Part_Size */
+
+/* ------------------------------------------------------------------ errors / device */
+
+/* Human-readable text for a status code (static storage). */
+EEG_API const char* eeg_status_string(eeg_status s);
+/* Detail of the last error raised on the calling thread (thread-local, "" if none). */
+EEG_API const char* eeg_last_error(void);
+/* Library version string. */
+EEG_API const char* eeg_version(void);
+/* Number of visible CUDA devices (0 when none); never fails. */
+EEG_API int eeg_device_count(void);
+/* Select the device used by the calling thread (reference: --device -> cudaSetDevice). */
+EEG_API eeg_status eeg_set_device(int device);
+/* Managed (unified) memory for the --um path (reference: cudaMallocManaged in src/um_graph.cu). */
+EEG_API eeg_status eeg_managed_alloc(size_t bytes, void** out);
+EEG_API void eeg_managed_free(void* p);
+
+/* ------------------------------------------------------------------ host edge list (Graph) */
+
+/* Host edge list produced by the loader or from caller arrays. Replaces `Graph`
+ * (include/graph.hpp:28-50). Ids are stored as read; has_zero_id tells whether the file is
+ * 0-based (otherwise the virtual-graph build shifts every id down by one, as
+ * VirtualGraph::VirtualGraph does at src/virtual_graph.cpp:5-12). */
+typedef struct eeg_graph eeg_graph;
+
+typedef struct eeg_graph_view {
+    uint32_t num_nodes;      /* max id (+1 when an id 0 exists) -- src/graph.cpp:102-105 */
+    uint64_t num_edges;
+    int has_zero_id;
+    int is_weighted;
+    const uint32_t* src;     /* num_edges source ids (as read) */
+    const uint32_t* dst;     /* num_edges destination ids (as read) */
+    const uint32_t* weight;  /* num_edges weights (1 when the column is absent); NULL if unweighted */
+} eeg_graph_view;
+
+/* Parse a text edge list (.edges .el .wel .txt .edgelist) with the rules of
+ * Graph::ReadGraph (src/graph.cpp:35-105): lines whose first character is not a digit are
+ * skipped, the third column is the weight (1 when absent), extra columns are ignored. Binary
+ * .bcsr/.bwcsr files (Subway's CSR format) are read too. n_threads<=0 picks the hardware count. */
+EEG_API eeg_status eeg_graph_load(const char* path, int weighted, int n_threads, eeg_graph** out);
+/* Wrap caller arrays (copied). ids are taken as 0-based; weight may be NULL (all 1). */
+EEG_API eeg_status eeg_graph_from_arrays(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src,
+                                         const uint32_t* dst, const uint32_t* weight, eeg_graph** out);
+EEG_API eeg_status eeg_graph_view_get(const eeg_graph* g, eeg_graph_view* out);
+/* Ids after the reference's 1-based -> 0-based normalisation (what the kernels see). */
+EEG_API eeg_status eeg_graph_normalized_ids(const eeg_graph* g, uint32_t* src_out, uint32_t* dst_out);
+EEG_API void eeg_graph_destroy(eeg_graph* g);
+
+/* Write a binary CSR file in Subway's .bcsr (unweighted) / .bwcsr (weighted) layout. */
+EEG_API eeg_status eeg_graph_save_bcsr(const eeg_graph* g, const char* path);
+
+/* ------------------------------------------------------------------ synthetic inputs */
+
+/* R-MAT edge generator (Graph500 quadrant recursion, counter-based RNG: deterministic,
+ * independent of thread count). Writes m = edge_factor << scale edges into caller arrays;
+ * weights uniform in [wmin, wmax] (weight may be NULL). Ids are 0-based, not permuted;
+ * duplicates and self-loops are kept. */
+EEG_API eeg_status eeg_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                                uint64_t seed, uint32_t wmin, uint32_t wmax, uint32_t* src, uint32_t* dst,
+                                uint32_t* weight);
+/* 2-D grid road-like graph: side x side vertices, 4-neighbour undirected (both arcs stored),
+ * each undirected edge deleted with probability p_delete, plus round(shortcut_frac * #grid edges)
+ * random undirected long-range shortcuts; weights uniform in [wmin, wmax].
+ * Call with src == NULL to obtain the arc count in *num_arcs first. */
+EEG_API eeg_status eeg_gen_grid(uint32_t side, double p_delete, double shortcut_frac, uint64_t seed,
+                                uint32_t wmin, uint32_t wmax, uint64_t* num_arcs, uint32_t* src,
+                                uint32_t* dst, uint32_t* weight);
+/* Symmetrise an arc list: out = in + reversed(in) (2*m arcs, caller arrays). */
+EEG_API eeg_status eeg_symmetrize(uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                                  uint32_t* src_out, uint32_t* dst_out, uint32_t* w_out);
+
+/* ------------------------------------------------------------------ device virtual graph */
+
+/* K-bounded virtual graph resident in HBM (replaces VirtualGraph / UMVirtualGraph).
+ * Layout: vertex v owns parts vstart[v] .. vstart[v+1]-1, part p holds up to K consecutive
+ * out-edges of vowner[p] in vcol[p*K .. p*K+K) (unused slots = 0xFFFFFFFF) and their weights
+ * in vw[]. Lossless: every edge is kept (the reference drops edges, src/virtual_graph.cpp:86-88). */
+typedef struct eeg_vgraph eeg_vgraph;
+
+enum {
+    EEG_VG_REVERSE = 1u << 0,   /* also build the in-edge (transposed) virtual graph (PageRank pull) */
+    EEG_VG_MANAGED = 1u << 1,   /* allocate in managed memory (the --um path) */
+    EEG_VG_INPUT_DEVICE = 1u << 2, /* src/dst/weight pointers are device (or managed) pointers */
+    EEG_VG_SHIFT_ONE = 1u << 3  /* subtract 1 from every id while building (1-based input) */
+};
+
+typedef struct eeg_vgraph_info {
+    uint32_t num_nodes;
+    uint64_t num_edges;
+    uint32_t K;
+    uint64_t num_parts;        /* sum_v ceil(outdeg(v)/K) -- numParts of the reference */
+    uint64_t num_rparts;       /* parts of the transposed graph (0 when not built) */
+    uint32_t max_out_degree;
+    uint32_t max_degree_vertex; /* lowest id with the largest out-degree */
+    uint64_t device_bytes;     /* HBM held by the graph */
+    float build_ms;            /* device time of the last build (CUDA events) */
+} eeg_vgraph_info;
+
+/* Build from a host edge list. The build runs on the GPU (degree histogram, part-count
+ * scan, scatter into the part-major layout, owner table by max-scan). `stream` is a
+ * cudaStream_t (NULL = legacy default stream). */
+EEG_API eeg_status eeg_vgraph_build(const eeg_graph* g, uint32_t K, uint32_t flags, void* stream, eeg_vgraph** out);
+/* Build from raw arrays (host or, with EEG_VG_INPUT_DEVICE, device pointers); weight may be NULL. */
+EEG_API eeg_status eeg_vgraph_build_arrays(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src,
+                                           const uint32_t* dst, const uint32_t* weight, uint32_t K,
+                                           uint32_t flags, void* stream, eeg_vgraph** out);
+EEG_API eeg_status eeg_vgraph_get_info(const eeg_vgraph* vg, eeg_vgraph_info* out);
+/* Copy the device arrays back (any pointer may be NULL to skip it). Sizes: vstart n+1,
+ * vowner num_parts, vcol/vw num_parts*K, outdeg n. */
+EEG_API eeg_status eeg_vgraph_download(const eeg_vgraph* vg, uint32_t* vstart, uint32_t* vowner, uint32_t* vcol,
+                                       uint32_t* vw, uint32_t* outdeg);
+/* Export the reference's host layout (src/virtual_graph.cpp:36-112, but lossless):
+ * nodePointer[n], edgeList[2m+n] = per vertex [deg, (t0,w0), (t1,w1) ...],
+ * partNodePointer[2*numParts] = {node, part} pairs. Any pointer may be NULL. */
+EEG_API eeg_status eeg_vgraph_export_reference_layout(const eeg_vgraph* vg, uint32_t* nodePointer,
+                                                      uint32_t* edgeList, uint32_t* partNodePointer);
+EEG_API void eeg_vgraph_destroy(eeg_vgraph* vg);
+
+/* ------------------------------------------------------------------ runs */
+
+typedef struct eeg_options {
+    uint32_t max_iterations;  /* 0 = default cap (n+2 for traversals, 10000 for PageRank) */
+    float pr_tolerance;       /* PageRank stop: bound on ||x - x*||_1 / ||x||_1 (0 = 1e-7) */
+    float pr_damping;         /* 0 = 0.85 (src/pr.cu:43) */
+    float pr_accuracy;        /* DD PageRank activation threshold on |delta| (0 = derived from tolerance) */
+    uint32_t block_size;      /* 0 = 512 threads per CTA */
+    uint32_t blocks_per_sm;   /* 0 = as many as occupancy allows */
+    uint32_t record_activity; /* 1: store active-vertex counts per iteration (reference --activity) */
+    uint32_t timeout_ms;      /* bound on any device-side wait (0 = 10000 ms) */
+    uint32_t reserved[8];
+} eeg_options;
+
+typedef struct eeg_result {
+    float kernel_ms;            /* CUDA-event time of the device work (init + persistent loop) */
+    uint32_t iterations;        /* rounds of the persistent loop (PageRank: sweeps) */
+    uint64_t reached_vertices;  /* n_r: vertices with a final value != initial "unreached" value */
+    uint64_t reached_edges;     /* m_r: out-edges of reached vertices (Graph500 TEPS count) */
+    uint64_t parts_processed;   /* virtual nodes expanded over the whole run */
+    uint64_t edges_scanned;     /* edge slots read over the whole run (redundant work included) */
+    uint64_t updates;           /* successful atomic improvements */
+    double algorithmic_bytes;   /* work-minimal byte count (12 n_r + (12|8) m_r; PR: sweeps*(12n+8m)) */
+    double gteps;               /* m_r / kernel time (PR: sweeps * m / time) */
+    double pr_residual;         /* PageRank: last ||x_{k+1}-x_k||_1 (FP64) */
+    double pr_l1_norm;          /* PageRank: ||x||_1 (FP64) */
+    uint32_t num_activity;      /* entries written to activity[] */
+    uint32_t launches;          /* kernels this call launched (persistent kernel + set-up/statistics) */
+    uint32_t reserved[6];
+} eeg_result;
+
+/* Default options (all zero fields -> defaults). */
+EEG_API void eeg_options_init(eeg_options* o);
+
+/* One run of `algo` / `variant` on a device virtual graph.
+ *  source      start vertex (ignored by PageRank; by CC except for SYNC_PUSH_DD, which seeds only it
+ *              -- src/eegraph.cu:548-553)
+ *  out         caller-owned result array of num_nodes entries: uint32 for BFS/SSSP/SSWP/CC,
+ *              float for PageRank; host memory unless out_on_device != 0
+ *  activity    optional (may be NULL) host array of `activity_cap` uint32 receiving the number of
+ *              active vertices per iteration (the reference's --activity sumLabels vector)
+ * Results: BFS hop levels, SSSP Dijkstra distances, SSWP widest-path values, CC min-plus labels,
+ * unreached = EEG_DIST_INFINITY (SSWP: 0, source = EEG_DIST_INFINITY). Every variant and K gives the
+ * same integer array. */
+EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, uint32_t source,
+                           const eeg_options* opts, void* out, int out_on_device, uint32_t* activity,
+                           uint32_t activity_cap, void* stream, eeg_result* res);
+
+/* ------------------------------------------------------------------ energy (NVML) */
+
+/* GPU energy over a region, from NVML's total-energy counter (mJ) with a power-sampling
+ * fallback. NVML is loaded at run time; without it eeg_energy_begin returns EEG_ERR_ENERGY and
+ * the caller reports "energy unavailable". csv_path may be NULL (no power trace). */
+typedef struct eeg_energy eeg_energy;
+EEG_API eeg_status eeg_energy_begin(int device, const char* csv_path, uint32_t sample_period_us, eeg_energy** out);
+EEG_API eeg_status eeg_energy_mark(eeg_energy* e);
+EEG_API eeg_status eeg_energy_end(eeg_energy* e, double* joules, double* seconds, double* avg_watts);
+EEG_API void eeg_energy_destroy(eeg_energy* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EEGRAPH_C_H */

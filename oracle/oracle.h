@@ -1,0 +1,74 @@
+/*
+ * oracle.h -- CPU oracle for the EEGraph push-kernel path. TEST INFRASTRUCTURE ONLY: tests, the
+ * smoke check and the bench's CPU baseline call it as the checker; the product never links it.
+ *
+ * Restates, in plain C, the reference's host-side algorithms (rwatling/EEGraph paths):
+ *   orc_parse_*          Graph::ReadGraph text rules             src/graph.cpp:35-105
+ *   orc_virtual_graph    VirtualGraph::MakeGraph layout           src/virtual_graph.cpp:36-112 (lossless)
+ *   orc_seq_sweep        {bfs,sssp,sswp,cc}::seq_cpu(VirtualGraph) src/bfs.cu:275-320, src/sssp.cu:357-404,
+ *                                                                 src/sswp.cu:273-320, src/cc.cu:329-376
+ *   orc_frontier_sweep   the *_push_dd kernels run sequentially   src/sssp.cu:192-299, host loop
+ *                                                                 src/eegraph.cu:89-211
+ *   orc_dijkstra / orc_bfs / orc_widest / orc_pagerank: independent textbook algorithms that pin the
+ *   fixed points (Dijkstra 1959; breadth-first search; max-min Dijkstra; power iteration in FP64).
+ * Parity pinned against the reference itself: oracle/_ref (built from the reference sources) and the
+ * golden vectors in tests/golden/ that it produced.
+ */
+#ifndef EEG_ORACLE_H
+#define EEG_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_INF 4294967294u
+
+enum { ORC_BFS = 0, ORC_SSSP = 1, ORC_SSWP = 2, ORC_CC = 3 };
+
+/* text edge-list parse, two calls: counts first, then fill (arrays of num_edges) */
+int orc_parse_count(const char* path, uint64_t* num_edges, uint32_t* num_nodes, int* has_zero_id);
+int orc_parse_fill(const char* path, int weighted, uint32_t* src, uint32_t* dst, uint32_t* w);
+
+/* number of parts = sum_v ceil(outdeg(v)/K) over 0-based edges */
+uint64_t orc_num_parts(uint32_t n, uint64_t m, const uint32_t* src, uint32_t K);
+/* reference layout (lossless): nodePointer[n], edgeList[2m+n], partNodePointer[2*numParts] */
+void orc_virtual_graph(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                       uint32_t K, uint32_t* nodePointer, uint32_t* edgeList, uint32_t* partNodePointer);
+
+/* initial values per the reference drivers: BFS/SSSP src=0 else INF; SSWP src=INF else 0; CC v */
+void orc_init_values(int algo, uint32_t n, uint32_t source, uint32_t* dist);
+
+/* Topology-driven sweeps over parts in order (the reference's seq_cpu). wrap != 0 keeps uint32 wrap
+ * of INF+w exactly as the reference; wrap == 0 skips unreached sources (the parity contract).
+ * dist must hold the initial values. Returns the number of sweeps, or -1 if max_sweeps is hit. */
+int64_t orc_seq_sweep(int algo, uint32_t n, uint64_t num_parts, const uint32_t* nodePointer, const uint32_t* edgeList,
+                      const uint32_t* partNodePointer, uint32_t K, int wrap, uint64_t max_sweeps, uint32_t* dist);
+
+/* Data-driven rounds (sync_push_dd / async_push_dd semantics), sequential: label1 = active set
+ * (all vertices when seed_all, else {source}), in-place relaxation, improved targets -> label2. */
+int64_t orc_frontier_sweep(int algo, uint32_t n, uint64_t num_parts, const uint32_t* nodePointer,
+                           const uint32_t* edgeList, const uint32_t* partNodePointer, uint32_t K, int seed_all,
+                           uint32_t source, uint32_t* dist);
+
+/* independent oracles over a 0-based edge list */
+void orc_bfs(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, uint32_t source, uint32_t* dist);
+void orc_dijkstra(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                  uint32_t source, uint32_t* dist);
+void orc_widest(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                uint32_t source, uint32_t* out);
+/* min-plus label fixed point label(v) = min(v, min_u label(u)+w(u,v)), all vertices seeded
+ * (multi-source Dijkstra with source distances = ids) */
+void orc_cc_labels(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w, uint32_t* out);
+
+/* FP64 PageRank: x = (1-d) + d * A^T D^-1 x (dangling mass dropped), power iteration until
+ * ||x_{k+1}-x_k||_1 <= tol * ||x||_1. Returns iterations. */
+int64_t orc_pagerank(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, double damping, double tol,
+                     uint64_t max_iter, double* x);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,163 @@
+// ref_shim.cpp -- C entry points over the REFERENCE's own host code, compiled from its sources by
+// oracle/Makefile into oracle/_ref/libref.so. TEST INFRASTRUCTURE ONLY: used to pin the oracle and to
+// produce the golden vectors in tests/golden/.
+//
+// Calls, unmodified: Graph::ReadGraph (src/graph.cpp:12-113), VirtualGraph::VirtualGraph and
+// VirtualGraph::MakeGraph (src/virtual_graph.cpp:3-112), {bfs,sssp,sswp,cc}::seq_cpu(VirtualGraph, uint*)
+// (src/bfs.cu:275, src/sssp.cu:357, src/sswp.cu:273, src/cc.cu:329).
+//
+// Two defects of MakeGraph are neutralised from the outside so that its own code yields the
+// lossless layout: (1) its per-source counter array comes from `new uint[n]` without zeroing
+// (src/virtual_graph.cpp:66) -- the replacement operator new[] below returns zeroed memory;
+// (2) it drops edges whose slot index reaches num_edges (:86-88) -- the Graph handed to it carries
+// 2m+n extra edges whose source is out of range, which the constructor and MakeGraph skip (:25, :78),
+// so the bound num_edges exceeds every real slot index.
+#include <chrono>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <iostream>
+#include <new>
+#include <sstream>
+
+#include "bfs.cuh"
+#include "cc.cuh"
+#include "graph.hpp"
+#include "sssp.cuh"
+#include "sswp.cuh"
+#include "virtual_graph.hpp"
+
+void* operator new[](size_t sz) {
+    void* p = calloc(1, sz ? sz : 1);
+    if (!p) abort();
+    return p;
+}
+void operator delete[](void* p) noexcept { free(p); }
+void operator delete[](void* p, size_t) noexcept { free(p); }
+
+namespace {
+
+struct Built {
+    Graph g;
+    VirtualGraph* vg = nullptr;
+    Built() : g(std::string("ref_shim.el"), true) {}
+    ~Built() {
+        // MakeGraph's arrays are never freed by the reference; release them here
+        if (vg) {
+            delete[] vg->edgeList;
+            delete[] vg->nodePointer;
+            delete[] vg->inDegree;
+            delete[] vg->outDegree;
+            delete[] vg->partNodePointer;
+            delete vg;
+        }
+    }
+};
+
+Built* make(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w) {
+    Built* b = new Built();
+    const uint64_t pad = 2 * m + n;
+    b->g.num_nodes = n;
+    b->g.hasZeroID = true;  // arrays are 0-based: the constructor must not shift
+    b->g.graphLoaded = true;
+    b->g.edges.resize(m + pad);
+    b->g.weights.resize(m + pad);
+    for (uint64_t e = 0; e < m; ++e) {
+        b->g.edges[e].source = src[e];
+        b->g.edges[e].end = dst[e];
+        b->g.weights[e] = w ? w[e] : 1u;
+    }
+    for (uint64_t e = m; e < m + pad; ++e) {
+        b->g.edges[e].source = n;  // out of range: skipped by the reference's bounds checks
+        b->g.edges[e].end = n;
+        b->g.weights[e] = 1u;
+    }
+    b->g.num_edges = (uint)(m + pad);
+    std::streambuf* old = std::cout.rdbuf();
+    std::ostringstream sink;
+    std::cout.rdbuf(sink.rdbuf());
+    b->vg = new VirtualGraph(b->g);
+    b->vg->MakeGraph();
+    std::cout.rdbuf(old);
+    return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Graph::ReadGraph on a file: returns a handle; ref_graph_copy fills caller arrays.
+void* ref_graph_read(const char* path, int weighted) {
+    Graph* g = new Graph(std::string(path), weighted != 0);
+    std::streambuf* old = std::cout.rdbuf();
+    std::ostringstream sink;
+    std::cout.rdbuf(sink.rdbuf());
+    g->ReadGraph();
+    std::cout.rdbuf(old);
+    return g;
+}
+void ref_graph_info(void* h, uint32_t* n, uint64_t* m, int* zero, uint64_t* nweights) {
+    Graph* g = (Graph*)h;
+    *n = g->num_nodes;
+    *m = g->num_edges;
+    *zero = g->hasZeroID ? 1 : 0;
+    *nweights = g->weights.size();
+}
+void ref_graph_copy(void* h, uint32_t* src, uint32_t* dst, uint32_t* w) {
+    Graph* g = (Graph*)h;
+    for (size_t e = 0; e < g->edges.size(); ++e) {
+        src[e] = g->edges[e].source;
+        dst[e] = g->edges[e].end;
+    }
+    if (w)
+        for (size_t e = 0; e < g->weights.size(); ++e) w[e] = g->weights[e];
+}
+void ref_graph_free(void* h) { delete (Graph*)h; }
+
+// VirtualGraph::MakeGraph layout: nodePointer[n], edgeList[2m+n], partNodePointer[2*numParts].
+uint64_t ref_num_parts(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w) {
+    Built* b = make(n, m, src, dst, w);
+    const uint64_t p = b->vg->numParts;
+    delete b;
+    return p;
+}
+void ref_virtual_graph(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                       uint32_t* nodePointer, uint32_t* edgeList, uint32_t* partNodePointer) {
+    Built* b = make(n, m, src, dst, w);
+    memcpy(nodePointer, b->vg->nodePointer, sizeof(uint32_t) * n);
+    memcpy(edgeList, b->vg->edgeList, sizeof(uint32_t) * (2 * m + n));
+    for (uint64_t p = 0; p < b->vg->numParts; ++p) {
+        partNodePointer[2 * p] = b->vg->partNodePointer[p].node;
+        partNodePointer[2 * p + 1] = b->vg->partNodePointer[p].part;
+    }
+    delete b;
+}
+
+// seq_cpu(VirtualGraph) with the reference drivers' initial values. algo: 0 BFS, 1 SSSP, 2 SSWP, 3 CC.
+// Part_Size is the reference's compile-time K = 8.
+// *seconds (may be null) receives the time of the seq_cpu call alone.
+int ref_seq_cpu(int algo, uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w,
+                uint32_t source, uint32_t* dist, double* seconds) {
+    if (n == 0 || source >= n) return -1;
+    Built* b = make(n, m, src, dst, w);
+    for (uint32_t v = 0; v < n; ++v) {
+        if (algo == 3) dist[v] = v;
+        else if (algo == 2) dist[v] = v == source ? DIST_INFINITY : 0u;
+        else dist[v] = v == source ? 0u : DIST_INFINITY;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    switch (algo) {
+        case 0: bfs::seq_cpu(*b->vg, dist); break;
+        case 1: sssp::seq_cpu(*b->vg, dist); break;
+        case 2: sswp::seq_cpu(*b->vg, dist); break;
+        case 3: cc::seq_cpu(*b->vg, dist); break;
+        default: delete b; return -1;
+    }
+    if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    delete b;
+    return 0;
+}
+
+uint32_t ref_part_size(void) { return Part_Size; }
+
+}  // extern "C"

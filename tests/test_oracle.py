@@ -1,0 +1,108 @@
+"""The oracle is pinned before it is trusted (CPU only).
+
+* against the golden vectors produced by the reference's own code (tests/golden/make_golden.py);
+* against the reference library itself on fresh seeded graphs, when oracle/_ref is built here;
+* the no-wrap restatement against independent textbook oracles (BFS, Dijkstra, widest path,
+  multi-source Dijkstra for the min-plus labels), which is the parity contract for the GPU.
+"""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def _cases():
+    z = np.load(GOLD / "seq_cpu.npz")
+    for name in z["names"]:
+        name = str(name)
+        yield name, {k.split(".", 1)[1]: z[k] for k in z.files if k.startswith(name + ".")}
+
+
+CASES = list(_cases())
+
+
+@pytest.mark.parametrize("name,c", CASES, ids=[n for n, _ in CASES])
+@pytest.mark.parametrize("algo", ["bfs", "sssp", "sswp", "cc"])
+def test_restatement_matches_reference_golden(name, c, algo):
+    n, s = int(c["n"][0]), int(c["source"][0])
+    got, _ = oracle.seq_sweep(algo, n, c["src"], c["dst"], c["w"], s, K=8, wrap=True)
+    assert np.array_equal(got, c[f"ref_{algo}"])
+
+
+@pytest.mark.parametrize("name,c", CASES, ids=[n for n, _ in CASES])
+def test_unit_weight_sssp_reference_equals_dijkstra(name, c):
+    n, s = int(c["n"][0]), int(c["source"][0])
+    want = oracle.dijkstra(n, c["src"], c["dst"], np.ones_like(c["w"]), s)
+    assert np.array_equal(c["ref_sssp_unit"], want)
+
+
+@pytest.mark.parametrize("name,c", CASES, ids=[n for n, _ in CASES])
+@pytest.mark.parametrize("algo", ["bfs", "sssp", "sswp", "cc"])
+def test_contract_equals_independent_oracles(name, c, algo):
+    n, s = int(c["n"][0]), int(c["source"][0])
+    got, _ = oracle.seq_sweep(algo, n, c["src"], c["dst"], c["w"], s, K=8, wrap=False)
+    want = oracle.expected(algo, "async_push_td", n, c["src"], c["dst"], c["w"], s)
+    assert np.array_equal(got, want)
+    if algo != "sssp":  # only SSSP differs from the reference (its INF+w wrap)
+        assert np.array_equal(got, c[f"ref_{algo}"])
+
+
+@pytest.mark.parametrize("name,c", CASES, ids=[n for n, _ in CASES])
+@pytest.mark.parametrize("K", [4, 8, 16])
+def test_frontier_rounds_reach_same_fixed_point(name, c, K):
+    n, s = int(c["n"][0]), int(c["source"][0])
+    for algo in ("bfs", "sssp", "sswp"):
+        got, _ = oracle.frontier_sweep(algo, n, c["src"], c["dst"], c["w"], s, K=K, seed_all=False)
+        assert np.array_equal(got, oracle.expected(algo, "sync_push_dd", n, c["src"], c["dst"], c["w"], s))
+    all_seeded, _ = oracle.frontier_sweep("cc", n, c["src"], c["dst"], c["w"], s, K=K, seed_all=True)
+    assert np.array_equal(all_seeded, oracle.cc_labels(n, c["src"], c["dst"], c["w"]))
+
+
+def test_layout_matches_reference_golden():
+    z = np.load(GOLD / "layout.npz")
+    cases = dict(CASES)
+    for name in ("hub", "rmat8"):
+        c = cases[name]
+        npn, el, pnp = oracle.virtual_graph(int(c["n"][0]), c["src"], c["dst"], c["w"], 8)
+        assert np.array_equal(npn, z[f"{name}.nodePointer"])
+        assert np.array_equal(el, z[f"{name}.edgeList"])
+        assert np.array_equal(pnp, z[f"{name}.partNodePointer"])
+
+
+def test_cc_source_seeded_differs_from_all_seeded():
+    # src/eegraph.cu:548-553: SYNC_PUSH_DD seeds only the source, so its CC fixed point differs
+    c = dict(CASES)["rmat10"]
+    n, s = int(c["n"][0]), int(c["source"][0])
+    a = oracle.expected("cc", "sync_push_dd", n, c["src"], c["dst"], c["w"], s)
+    b = oracle.expected("cc", "async_push_td", n, c["src"], c["dst"], c["w"], s)
+    assert not np.array_equal(a, b)
+    assert np.all(a >= b)
+
+
+def test_pagerank_oracle_fixed_point():
+    c = dict(CASES)["rmat10"]
+    n = int(c["n"][0])
+    x, it = oracle.pagerank(n, c["src"], c["dst"], 0.85, 1e-15)
+    deg = np.bincount(c["src"], minlength=n).astype(np.float64)
+    contrib = np.where(deg > 0, x / np.maximum(deg, 1), 0.0)
+    y = np.zeros(n)
+    np.add.at(y, c["dst"], contrib[c["src"]])
+    assert np.abs(0.15 + 0.85 * y - x).sum() <= 1e-12 * x.sum()
+    assert it > 10
+
+
+@pytest.mark.skipif(not oracle.ref_available(), reason="reference library not built here")
+@pytest.mark.parametrize("seed", [21, 22, 23])
+def test_restatement_matches_reference_library(seed):
+    import eegraph_gb300 as E
+
+    s, d, w = E.gen_rmat(9, 8, seed=seed, wmin=1, wmax=63)
+    n = 512
+    src = int(np.bincount(s, minlength=n).argmax())
+    for algo in ("bfs", "sssp", "sswp", "cc"):
+        got, _ = oracle.seq_sweep(algo, n, s, d, w, src, K=8, wrap=True)
+        assert np.array_equal(got, oracle.ref_seq_cpu(algo, n, s, d, w, src))
