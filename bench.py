@@ -232,7 +232,7 @@ def bench_gpu(args) -> None:
            {"s": s, "d": d, "w": w, "ss": ss, "ds": ds, "ws": ws}.items()}
     host_out = {a: np.empty(n, np.float32 if a == "pr" else np.uint32) for a, _ in ALGO_PLAN}
     e2e_ms = []
-    for i in range(args.warmup + args.steps):
+    for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         g1 = E.VirtualGraph.build(n, pin["s"], pin["d"], pin["w"], K=args.k, reverse=True, stream=stream)
@@ -251,7 +251,7 @@ def bench_gpu(args) -> None:
         tt = torch.tensor([e2e_total_ms], dtype=torch.float64, device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_total_ms = float(tt[0])
-    e2e_value = total_edges_all / (e2e_total_ms * 1e-3) / 1e9
+    e2e_value = total_edges_all / (e2e_total_ms * 1e-3) / 1e9 if e2e_ms else None
     h2d = 4 * (3 * m + 3 * m_sym)
     d2h = 4 * n * len(ALGO_PLAN)
 
@@ -296,8 +296,8 @@ def bench_gpu(args) -> None:
         "roofline": {"bound": "hbm", "kernel": kern_name, "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": peak_kind,
                      "traffic": load_traffic(kern_name, f"s{scale}_k{args.k}")},
-        "e2e": {"value": round(e2e_value, 3), "unit": "GTEPS", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(e2e_total_ms / args.steps, 3)},
+        "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_total_ms / args.steps, 3)},
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
@@ -419,7 +419,12 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
+    ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
+                    help="subset of the step to run (profiling); the headline uses all five")
     args = ap.parse_args()
+    global ALGO_PLAN
+    ALGO_PLAN = [p for p in ALGO_PLAN if p[0] in args.algos.split(",")]
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

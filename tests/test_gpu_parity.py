@@ -130,19 +130,20 @@ def test_builder_layout(gpu):
             # each vertex's slots hold exactly its out-edges (any order), padding = 0xFFFFFFFF
             vcol, vw = lay["vcol"].reshape(-1), lay["vw"].reshape(-1)
             order = np.argsort(s, kind="stable")
-            starts = np.concatenate([[0], np.cumsum(deg)])
+            starts = np.concatenate([[0], np.cumsum(deg, dtype=np.int64)])
             for v in np.flatnonzero(deg)[:500]:
-                a, b = lay["vstart"][v] * K, lay["vstart"][v] * K + deg[v]
+                a = int(lay["vstart"][v]) * K
+                b = a + int(deg[v])
                 got = sorted(zip(vcol[a:b].tolist(), vw[a:b].tolist()))
                 idx = order[starts[v]:starts[v + 1]]
                 assert got == sorted(zip(d[idx].tolist(), w[idx].tolist()))
-                assert np.all(vcol[b:lay["vstart"][v + 1] * K] == 0xFFFFFFFF)
+                assert np.all(vcol[b:int(lay["vstart"][v + 1]) * K] == 0xFFFFFFFF)
             # reference layout export: nodePointer / partNodePointer exact, edges per vertex as a multiset
             npn, el, pnp = vg.reference_layout()
             onp, oel, opnp = oracle.virtual_graph(n, s, d, w, K)
             assert np.array_equal(npn, onp) and np.array_equal(pnp, opnp)
             for v in range(0, n, 37):
-                p, dv = npn[v], el[npn[v]]
+                p, dv = int(npn[v]), int(el[npn[v]])
                 assert dv == oel[p]
                 pairs = sorted(zip(el[p + 1:p + 1 + 2 * dv:2].tolist(), el[p + 2:p + 2 + 2 * dv:2].tolist()))
                 opairs = sorted(zip(oel[p + 1:p + 1 + 2 * dv:2].tolist(), oel[p + 2:p + 2 + 2 * dv:2].tolist()))
