@@ -73,7 +73,7 @@ static void free_ws(eeg_vgraph* vg) {
     vg_free(vg, w.contrib[0]);
     vg_free(vg, w.contrib[1]);
     vg_free(vg, w.acc);
-    vg_free(vg, w.cross);
+    vg_free(vg, w.arrive);
     if (w.pctrl) cudaFree(w.pctrl);
     if (w.stats) cudaFree(w.stats);
     if (w.ev[0]) cudaEventDestroy(w.ev[0]);

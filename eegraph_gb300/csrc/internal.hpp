@@ -51,6 +51,7 @@ struct PRCtrl {
     double last_resid;
     double last_norm;
     unsigned long long edges_scanned;
+    unsigned long long zero_in;  // vertices without in-edges (value stays 1-d)
 };
 
 struct Workspace {
@@ -65,10 +66,7 @@ struct Workspace {
     float* x = nullptr;           // n
     float* contrib[2] = {nullptr, nullptr};  // n each
     double* acc = nullptr;        // n (partials of vertices whose parts cross warp chunks)
-    uint32_t* cross = nullptr;    // list of those vertices
-    uint32_t ncross = 0;
-    unsigned long long zero_in = 0;  // vertices with no in-edges
-    double zero_in_norm = 0.0;    // their constant share of ||x||_1
+    uint32_t* arrive = nullptr;   // n (chunks that delivered a partial, per vertex)
     PRCtrl* pctrl = nullptr;
     // misc
     unsigned long long* stats = nullptr;  // reached counters

@@ -7,15 +7,20 @@
 // over-counts vertices with more than K out-edges; here each vertex is updated exactly once per sweep.
 //
 // GB300 form: Jacobi sweeps that PULL over the transposed virtual graph (parts of <= K in-edges).
-// A warp owns 32 consecutive parts: each lane sums its part with a compensated (two-sum) FP32
-// accumulation of contrib[u] = x_u / outdeg(u); parts of one vertex are combined by a segmented
-// warp scan; a vertex whose parts all sit in the warp's chunk is finalised in place, a vertex whose
-// parts span chunks adds its pair sum to an FP64 slot that a second phase finalises. The stop test
-// uses FP64 reductions: ||x_{k+1}-x_k||_1 * d/(1-d) <= tol * ||x_{k+1}||_1 bounds the distance to the
-// fixed point (the Jacobi map contracts by d in the L1 norm).
-//   SYNC variants: contrib double-buffered (deterministic Jacobi).
-//   ASYNC variants: contrib updated in place (Gauss-Seidel-like: values of this sweep are used as
-//   soon as they are written; same fixed point, fewer sweeps, order-dependent rounding).
+//  * A warp owns chunks of 32 consecutive parts and keeps two chunks in flight: their part rows
+//    (256-bit loads) and then all 2*K gathers of contrib[u] = x_u / outdeg(u) are issued before any
+//    of them is consumed; the old value and out-degree of each chunk's segment ends are prefetched
+//    alongside the gathers.
+//  * Each lane sums its part with a compensated (two-sum) FP32 accumulation; parts of one vertex are
+//    combined by a segmented warp scan of (hi, lo) pairs.
+//  * A vertex whose parts all sit in one chunk is finalised in place. A vertex whose parts span chunks
+//    gets one FP64 atomic partial per chunk plus an arrival count; the warp that brings the count to
+//    the number of chunks spanned finalises it. So a sweep needs ONE grid barrier.
+//  * Stop test in FP64: ||x_{k+1}-x_k||_1 * d/(1-d) <= tol * ||x_{k+1}||_1 bounds the distance to the
+//    fixed point (the Jacobi map contracts by d in the L1 norm).
+//   SYNC variants: contrib double-buffered (deterministic Jacobi up to the FP64 partial order).
+//   ASYNC variants: contrib updated in place (values of this sweep are used as soon as written; same
+//   fixed point, fewer sweeps, order-dependent rounding).
 #include <algorithm>
 #include <cmath>
 
@@ -25,6 +30,11 @@ namespace eeg {
 namespace {
 
 constexpr int PR_TPB = 512;
+// chunks in flight per warp (K = 16 keeps one: its 16 ids + 16 gathered values already fill the registers)
+template <int K>
+struct InFlight {
+    static constexpr int U = K >= 16 ? 1 : 2;
+};
 
 struct PRArgs {
     uint32_t n;
@@ -36,15 +46,13 @@ struct PRArgs {
     float* x;
     float* c0;
     float* c1;
-    double* acc;
-    const uint32_t* __restrict__ cross;
-    uint32_t ncross;
+    double* acc;       // FP64 partial sums of vertices whose parts span chunks
+    uint32_t* arrive;  // chunks that have delivered their partial, per vertex
     uint32_t max_iters;
     PRCtrl* ctrl;
     float damping;
     float base;
     double tol;
-    double zero_in_norm;
     uint64_t timeout_ns;
     uint32_t inplace;
 };
@@ -64,20 +72,20 @@ __device__ __forceinline__ void pair_add(float& h1, float& l1, float h2, float l
     l1 = __fsub_rn(t, __fsub_rn(h1, s));
 }
 
-__device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, double sum, float* cnext, double& r,
-                                         double& nrm) {
+__device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, double sum, float xo, uint32_t od, float* cnext,
+                                         double& r, double& nrm) {
     const float xn = a.base + a.damping * (float)sum;
-    const float xo = __ldcg(&a.x[v]);
     r += fabs((double)xn - (double)xo);
     nrm += (double)xn;
     a.x[v] = xn;
-    const uint32_t od = __ldg(&a.outdeg[v]);
     cnext[v] = od ? xn / (float)od : 0.f;
 }
 
 template <int K>
-__global__ void __launch_bounds__(PR_TPB) k_pagerank(PRArgs a) {
+__global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
+    constexpr int PR_U = InFlight<K>::U;
     __shared__ double s_red[2][PR_TPB / 32];
+    __shared__ unsigned long long s_zero;
     PRCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * PR_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * PR_TPB;
@@ -87,6 +95,10 @@ __global__ void __launch_bounds__(PR_TPB) k_pagerank(PRArgs a) {
     const uint64_t pol = l2_evict_first_policy();
     uint32_t epoch = 0;
 
+    // ---- set-up: x0 = 1-d, contrib0, partial slots; count vertices without in-edges
+    if (threadIdx.x == 0) s_zero = 0;
+    __syncthreads();
+    unsigned long long zero_in = 0;
     for (uint32_t v = gtid; v < a.n; v += gthreads) {
         a.x[v] = a.base;
         const uint32_t od = a.outdeg[v];
@@ -94,110 +106,144 @@ __global__ void __launch_bounds__(PR_TPB) k_pagerank(PRArgs a) {
         a.c0[v] = c;
         a.c1[v] = c;
         a.acc[v] = 0.0;
+        a.arrive[v] = 0u;
+        zero_in += (a.rvstart[v + 1] == a.rvstart[v]) ? 1ull : 0ull;
     }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) zero_in += __shfl_down_sync(0xffffffffu, zero_in, off);
+    if (lane == 0 && zero_in) atomicAdd(&s_zero, zero_in);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_zero) atomicAdd(&ctrl->zero_in, s_zero);
     uint32_t s = 0;
     unsigned long long my_edges = 0;
     if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
+    {
+        const double zero_norm = (double)*(volatile unsigned long long*)&ctrl->zero_in * (double)a.base;
+        for (;; ++s) {
+            if (s >= a.max_iters) {
+                if (blockIdx.x == 0 && threadIdx.x == 0)
+                    atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_ITER_CAP);
+                break;
+            }
+            const uint32_t slot = s % 3u;
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                ctrl->resid[(s + 1u) % 3u] = 0.0;
+                ctrl->norm[(s + 1u) % 3u] = 0.0;
+            }
+            const float* __restrict__ ccur = (s & 1u) && !a.inplace ? a.c1 : a.c0;
+            float* cnext = a.inplace ? a.c0 : ((s & 1u) ? a.c0 : a.c1);
+            double r = 0.0, nrm = 0.0;
 
-    for (;; ++s) {
-        if (s >= a.max_iters) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_ITER_CAP);
-            break;
-        }
-        const uint32_t slot = s % 3u;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            ctrl->resid[(s + 1u) % 3u] = 0.0;
-            ctrl->norm[(s + 1u) % 3u] = 0.0;
-        }
-        const float* __restrict__ ccur = (s & 1u) && !a.inplace ? a.c1 : a.c0;
-        float* cnext = a.inplace ? a.c0 : ((s & 1u) ? a.c0 : a.c1);
-        double r = 0.0, nrm = 0.0;
-
-        // ---- phase P: pull over parts
-        for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
-            const uint32_t p = ch * 32u + lane;
-            const bool valid = p < a.RP;
-            uint32_t v = 0xFFFFFFFFu;
-            float hi = 0.f, lo = 0.f;
-            if (valid) {
-                v = __ldg(&a.rvowner[p]);
-                uint32_t col[K];
-                ld_part<K>(a.rvcol + (size_t)p * K, col, pol);
-                float y[K];
+            for (uint32_t base = gwarp; base < nchunks; base += nwarps * PR_U) {
+                uint32_t v[PR_U], col[PR_U][K];
+                bool valid[PR_U];
 #pragma unroll
-                for (int i = 0; i < K; ++i) y[i] = col[i] != NO_EDGE ? __ldcg(&ccur[col[i]]) : 0.f;
+                for (int u = 0; u < PR_U; ++u) {
+                    const uint32_t ch = base + (uint32_t)u * nwarps;
+                    const uint32_t p = ch * 32u + lane;
+                    valid[u] = ch < nchunks && p < a.RP;
+                    v[u] = 0xFFFFFFFFu;
+                    if (valid[u]) {
+                        v[u] = __ldg(&a.rvowner[p]);
+                        ld_part<K>(a.rvcol + (size_t)p * K, col[u], pol);
+                    }
+                }
+                float y[PR_U][K];
 #pragma unroll
-                for (int i = 0; i < K; ++i) {
-                    if (col[i] == NO_EDGE) break;
-                    ++my_edges;
-                    float t, e;
-                    two_sum(hi, y[i], t, e);
-                    hi = t;
-                    lo = __fadd_rn(lo, e);
+                for (int u = 0; u < PR_U; ++u)
+#pragma unroll
+                    for (int i = 0; i < K; ++i)
+                        y[u][i] = (valid[u] && col[u][i] != NO_EDGE) ? __ldcg(&ccur[col[u][i]]) : 0.f;
+                // segment ends: prefetch what finalisation needs while the gathers are in flight
+                bool last[PR_U];
+                float xo[PR_U];
+                uint32_t od[PR_U], vs0[PR_U], vs1[PR_U];
+#pragma unroll
+                for (int u = 0; u < PR_U; ++u) {
+                    const uint32_t vn = __shfl_down_sync(0xffffffffu, v[u], 1);
+                    last[u] = valid[u] && (lane == 31u || vn != v[u]);
+                    xo[u] = 0.f;
+                    od[u] = 0u;
+                    vs0[u] = vs1[u] = 0u;
+                    if (last[u]) {
+                        xo[u] = __ldcg(&a.x[v[u]]);
+                        od[u] = __ldg(&a.outdeg[v[u]]);
+                        vs0[u] = __ldg(&a.rvstart[v[u]]);
+                        vs1[u] = __ldg(&a.rvstart[v[u] + 1]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < PR_U; ++u) {
+                    float hi = 0.f, lo = 0.f;
+#pragma unroll
+                    for (int i = 0; i < K; ++i) {
+                        if (!valid[u] || col[u][i] == NO_EDGE) break;
+                        ++my_edges;
+                        float t, e;
+                        two_sum(hi, y[u][i], t, e);
+                        hi = t;
+                        lo = __fadd_rn(lo, e);
+                    }
+                    // segmented inclusive scan over lanes of the same vertex (a vertex's parts are contiguous)
+#pragma unroll
+                    for (int off = 1; off < 32; off <<= 1) {
+                        const uint32_t vo = __shfl_up_sync(0xffffffffu, v[u], off);
+                        const float ho = __shfl_up_sync(0xffffffffu, hi, off);
+                        const float lo2 = __shfl_up_sync(0xffffffffu, lo, off);
+                        if (lane >= (uint32_t)off && vo == v[u]) pair_add(hi, lo, ho, lo2);
+                    }
+                    if (last[u]) {
+                        const uint32_t ch = base + (uint32_t)u * nwarps;
+                        const uint32_t first_chunk = vs0[u] / 32u, last_chunk = (vs1[u] - 1u) / 32u;
+                        if (first_chunk == ch && last_chunk == ch) {
+                            finalize(a, v[u], (double)hi + (double)lo, xo[u], od[u], cnext, r, nrm);
+                        } else {
+                            atomicAdd(&a.acc[v[u]], (double)hi + (double)lo);
+                            __threadfence();
+                            const uint32_t need = last_chunk - first_chunk + 1u;
+                            if (atomicAdd(&a.arrive[v[u]], 1u) + 1u == need) {
+                                __threadfence();
+                                const unsigned long long bits =
+                                    atomicExch((unsigned long long*)&a.acc[v[u]], 0ull);
+                                a.arrive[v[u]] = 0u;
+                                finalize(a, v[u], __longlong_as_double((long long)bits), xo[u], od[u], cnext, r,
+                                         nrm);
+                            }
+                        }
+                    }
                 }
             }
-            // segmented inclusive scan over lanes holding the same vertex (parts of a vertex are contiguous)
+            // CTA reduction of the FP64 residual / norm, one atomic per CTA
 #pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const uint32_t vo = __shfl_up_sync(0xffffffffu, v, off);
-                const float ho = __shfl_up_sync(0xffffffffu, hi, off);
-                const float lo2 = __shfl_up_sync(0xffffffffu, lo, off);
-                if (lane >= (uint32_t)off && vo == v) pair_add(hi, lo, ho, lo2);
+            for (int off = 16; off > 0; off >>= 1) {
+                r += __shfl_down_sync(0xffffffffu, r, off);
+                nrm += __shfl_down_sync(0xffffffffu, nrm, off);
             }
-            const uint32_t vnext = __shfl_down_sync(0xffffffffu, v, 1);
-            const uint32_t vprev = __shfl_up_sync(0xffffffffu, v, 1);
-            const bool head = (lane == 0) || (vprev != v);
-            const uint32_t head_mask = __ballot_sync(0xffffffffu, head);
-            const bool last = (lane == 31) || (vnext != v);
-            if (valid && last) {
-                const uint32_t below = head_mask & (0xffffffffu >> (31u - lane));
-                const uint32_t head_lane = 31u - __clz(below);
-                bool complete = true;
-                if (head_lane == 0 && __ldg(&a.rvstart[v]) < ch * 32u) complete = false;
-                if (lane == 31 && __ldg(&a.rvstart[v + 1]) > ch * 32u + 32u) complete = false;
-                if (complete) finalize(a, v, (double)hi + (double)lo, cnext, r, nrm);
-                else atomicAdd(&a.acc[v], (double)hi + (double)lo);
+            if (lane == 0) {
+                s_red[0][threadIdx.x >> 5] = r;
+                s_red[1][threadIdx.x >> 5] = nrm;
             }
-        }
-        if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
-
-        // ---- phase F: vertices whose parts span warp chunks
-        for (uint32_t i = gtid; i < a.ncross; i += gthreads) {
-            const uint32_t v = a.cross[i];
-            const double sum = __ldcg(&a.acc[v]);
-            a.acc[v] = 0.0;
-            finalize(a, v, sum, cnext, r, nrm);
-        }
-        // block reduction of the FP64 residual / norm, one atomic per CTA
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) {
-            r += __shfl_down_sync(0xffffffffu, r, off);
-            nrm += __shfl_down_sync(0xffffffffu, nrm, off);
-        }
-        if (lane == 0) {
-            s_red[0][threadIdx.x >> 5] = r;
-            s_red[1][threadIdx.x >> 5] = nrm;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double rr = 0.0, nn = 0.0;
-            for (int w = 0; w < PR_TPB / 32; ++w) {
-                rr += s_red[0][w];
-                nn += s_red[1][w];
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double rr = 0.0, nn = 0.0;
+                for (int w = 0; w < PR_TPB / 32; ++w) {
+                    rr += s_red[0][w];
+                    nn += s_red[1][w];
+                }
+                atomicAdd(&ctrl->resid[slot], rr);
+                atomicAdd(&ctrl->norm[slot], nn);
             }
-            atomicAdd(&ctrl->resid[slot], rr);
-            atomicAdd(&ctrl->norm[slot], nn);
-        }
-        if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
-        const double resid = *(volatile double*)&ctrl->resid[slot];
-        const double norm = *(volatile double*)&ctrl->norm[slot] + a.zero_in_norm;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            ctrl->last_resid = resid;
-            ctrl->last_norm = norm;
-        }
-        if ((double)a.damping / (1.0 - (double)a.damping) * resid <= a.tol * norm) {
-            ++s;
-            break;
+            if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
+            const double resid = *(volatile double*)&ctrl->resid[slot];
+            const double norm = *(volatile double*)&ctrl->norm[slot] + zero_norm;
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                ctrl->last_resid = resid;
+                ctrl->last_norm = norm;
+            }
+            if ((double)a.damping / (1.0 - (double)a.damping) * resid <= a.tol * norm) {
+                ++s;
+                break;
+            }
         }
     }
 finish:
@@ -205,24 +251,6 @@ finish:
     for (int off = 16; off > 0; off >>= 1) my_edges += __shfl_down_sync(0xffffffffu, my_edges, off);
     if (lane == 0 && my_edges) atomicAdd(&ctrl->edges_scanned, my_edges);
     if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->iterations = s;
-}
-
-// Vertices whose in-parts are not inside one 32-part chunk, and the number of vertices without
-// in-edges (their value stays 1-d, a constant part of ||x||_1).
-__global__ void k_cross(const uint32_t* __restrict__ rvstart, uint32_t n, uint32_t* cross, uint32_t* ncross,
-                        unsigned long long* zero_in) {
-    unsigned long long z = 0;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const uint32_t a = rvstart[v], b = rvstart[v + 1];
-        if (b == a) {
-            ++z;
-            continue;
-        }
-        if (a / 32u != (b - 1u) / 32u) cross[atomicAdd(ncross, 1u)] = v;
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) z += __shfl_down_sync(0xffffffffu, z, off);
-    if ((threadIdx.x & 31u) == 0 && z) atomicAdd(zero_in, z);
 }
 
 template <int K>
@@ -247,33 +275,18 @@ eeg_status launch_pr(const PRArgs& args, int device, uint32_t bps, cudaStream_t 
 
 }  // namespace
 
-static eeg_status ensure_pr_ws(eeg_vgraph* vg, cudaStream_t st, uint32_t* launched) {
+static eeg_status ensure_pr_ws(eeg_vgraph* vg) {
     Workspace& ws = vg->ws;
     const size_t n = std::max<uint32_t>(vg->n, 1);
     if (!ws.x) EEG_TRY(vg_alloc(vg, (void**)&ws.x, sizeof(float) * n));
     if (!ws.contrib[0]) EEG_TRY(vg_alloc(vg, (void**)&ws.contrib[0], sizeof(float) * n));
     if (!ws.contrib[1]) EEG_TRY(vg_alloc(vg, (void**)&ws.contrib[1], sizeof(float) * n));
     if (!ws.acc) EEG_TRY(vg_alloc(vg, (void**)&ws.acc, sizeof(double) * n));
+    if (!ws.arrive) EEG_TRY(vg_alloc(vg, (void**)&ws.arrive, sizeof(uint32_t) * n));
     if (!ws.pctrl) EEG_CUDA(cudaMalloc((void**)&ws.pctrl, sizeof(PRCtrl)));
     if (!ws.ev[0]) {
         EEG_CUDA(cudaEventCreate(&ws.ev[0]));
         EEG_CUDA(cudaEventCreate(&ws.ev[1]));
-    }
-    if (!ws.cross) {
-        EEG_TRY(vg_alloc(vg, (void**)&ws.cross, sizeof(uint32_t) * n));
-        unsigned long long* cnt = nullptr;
-        EEG_CUDA(cudaMalloc((void**)&cnt, 16));
-        EEG_CUDA(cudaMemsetAsync(cnt, 0, 16, st));
-        const unsigned blocks = (unsigned)std::min<uint64_t>((vg->n + 255) / 256 + 1, (uint64_t)sm_count(vg->device) * 8);
-        k_cross<<<blocks, 256, 0, st>>>(vg->rev.vstart, vg->n, ws.cross, (uint32_t*)cnt, cnt + 1);
-        EEG_CUDA(cudaGetLastError());
-        unsigned long long h[2];
-        EEG_CUDA(cudaMemcpyAsync(h, cnt, 16, cudaMemcpyDeviceToHost, st));
-        EEG_CUDA(cudaStreamSynchronize(st));
-        ws.ncross = (uint32_t)(h[0] & 0xFFFFFFFFull);
-        ws.zero_in = h[1];
-        cudaFree(cnt);
-        *launched += 1;
     }
     return EEG_OK;
 }
@@ -288,12 +301,9 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
         set_last_error("empty graph");
         return EEG_ERR_INVALID;
     }
-    uint32_t launches = 1;  // the persistent kernel (+1 the first time: the chunk-crossing list)
-    EEG_TRY(ensure_pr_ws(vg, st, &launches));
+    EEG_TRY(ensure_pr_ws(vg));
     Workspace& ws = vg->ws;
     const float damping = o.pr_damping > 0.f ? o.pr_damping : 0.85f;
-    const float base = 1.0f - damping;
-    ws.zero_in_norm = (double)ws.zero_in * (double)base;
     EEG_CUDA(cudaMemsetAsync(ws.pctrl, 0, sizeof(PRCtrl), st));
     PRArgs a{};
     a.n = vg->n;
@@ -306,14 +316,12 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
     a.c0 = ws.contrib[0];
     a.c1 = ws.contrib[1];
     a.acc = ws.acc;
-    a.cross = ws.cross;
-    a.ncross = ws.ncross;
+    a.arrive = ws.arrive;
     a.max_iters = o.max_iterations ? o.max_iterations : 10000u;
     a.ctrl = ws.pctrl;
     a.damping = damping;
-    a.base = base;
+    a.base = 1.0f - damping;
     a.tol = o.pr_tolerance > 0.f ? (double)o.pr_tolerance : 1e-7;
-    a.zero_in_norm = ws.zero_in_norm;
     a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
     a.inplace = (variant == EEG_ASYNC_PUSH_TD || variant == EEG_ASYNC_PUSH_DD) ? 1u : 0u;
 
@@ -339,7 +347,7 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
         res->parts_processed = (uint64_t)hc.iterations * vg->rev.P;
         res->pr_residual = hc.last_resid;
         res->pr_l1_norm = hc.last_norm;
-        res->launches = launches;
+        res->launches = 1;
     }
     if (hc.bw.status == DEV_TIMEOUT) {
         set_last_error("grid barrier wait exceeded the timeout");

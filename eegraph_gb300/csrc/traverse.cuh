@@ -32,8 +32,6 @@ namespace eeg {
 namespace trav {
 
 constexpr int T_TPB = 512;
-constexpr int BIG_PARTS = 32;  // a claimed vertex with more parts is appended by the whole CTA
-constexpr int BIG_CAP = 64;
 
 struct TravArgs {
     uint32_t n;
@@ -85,21 +83,69 @@ __device__ __forceinline__ uint32_t atomic_improve(uint32_t* p, uint32_t v) {
     return OP == OP_SSWP ? atomicMax(p, v) : atomicMin(p, v);
 }
 
-struct BigEntry {
-    uint32_t first, count, dst;
-};
+constexpr int WCAP = 256;  // per-warp append buffer (claimed vertices) before a flush to the queue
+
+// Warp-cooperative append of the warp's claimed vertices to the next queue: one reservation per flush
+// (atomicAdd of the parts total), then every claimed vertex's part ids are written; a vertex with more
+// than 32 parts is written by the whole warp. Called by all 32 lanes with a warp-uniform `cnt`.
+__device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
+                                           uint32_t nxt, uint32_t lane) {
+    __syncwarp();
+    uint32_t sum = 0;
+    for (uint32_t e = lane; e < cnt; e += 32u) {
+        const uint32_t t = buf[e];
+        sum += a.vstart[t + 1] - a.vstart[t];
+    }
+    uint32_t inc = sum;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= (uint32_t)off) inc += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+    uint32_t base = 0;
+    if (lane == 0) {
+        if (total) base = atomicAdd(&a.ctrl->qparts[nxt], total);
+        atomicAdd(&a.ctrl->qverts[nxt], cnt);
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    uint32_t pos = base + inc - sum;
+    const uint32_t rounds = (cnt + 31u) / 32u;
+    for (uint32_t k = 0; k < rounds; ++k) {
+        const uint32_t e = k * 32u + lane;
+        uint32_t s0 = 0, np = 0;
+        if (e < cnt) {
+            const uint32_t t = buf[e];
+            s0 = a.vstart[t];
+            np = a.vstart[t + 1] - s0;
+            if (np <= 32u)
+                for (uint32_t j = 0; j < np; ++j) qnext[pos + j] = s0 + j;
+        }
+        uint32_t big = __ballot_sync(0xffffffffu, np > 32u);
+        while (big) {  // hub vertices: the whole warp writes their part ids
+            const int l = __ffs(big) - 1;
+            big &= big - 1u;
+            const uint32_t bs0 = __shfl_sync(0xffffffffu, s0, l);
+            const uint32_t bnp = __shfl_sync(0xffffffffu, np, l);
+            const uint32_t bpos = __shfl_sync(0xffffffffu, pos, l);
+            for (uint32_t j = lane; j < bnp; j += 32u) qnext[bpos + j] = bs0 + j;
+        }
+        pos += np;
+    }
+    __syncwarp();
+}
 
 template <int OP, int K, bool TD>
-__global__ void __launch_bounds__(T_TPB) k_traverse(TravArgs a) {
-    constexpr int ACT_CAP = T_TPB * K;
-    __shared__ uint32_t s_act[TD ? 1 : ACT_CAP];
-    __shared__ uint32_t s_warp[33];
-    __shared__ uint32_t s_cnt, s_base, s_nbig;
-    __shared__ BigEntry s_big[TD ? 1 : BIG_CAP];
+__global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
+    __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
 
     TravCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * T_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * T_TPB;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gwarp = gtid >> 5, nwarps = gthreads >> 5;
+    const uint32_t lanemask_lt = (1u << lane) - 1u;
+    uint32_t* wbuf = s_buf[TD ? 0 : threadIdx.x >> 5];
     const uint64_t pol = l2_evict_first_policy();
     uint32_t epoch = 0;
 
@@ -115,10 +161,6 @@ __global__ void __launch_bounds__(T_TPB) k_traverse(TravArgs a) {
             ctrl->qparts[0] = s1 - s0;
             ctrl->qverts[0] = 1u;
         }
-    }
-    if (threadIdx.x == 0) {
-        s_cnt = 0;
-        s_nbig = 0;
     }
     unsigned long long my_parts = 0, my_edges = 0, my_updates = 0;
     uint32_t it = 0;
@@ -150,91 +192,68 @@ __global__ void __launch_bounds__(T_TPB) k_traverse(TravArgs a) {
         uint32_t* __restrict__ qnext = (it & 1u) ? a.q0 : a.q1;
         const uint32_t tag = it + 1u;
         uint32_t changed = 0;
+        uint32_t wcnt = 0;  // warp-uniform fill of wbuf
 
-        for (uint32_t base = blockIdx.x * T_TPB; base < len; base += gthreads) {
-            const uint32_t idx = base + threadIdx.x;
+        for (uint32_t wb = gwarp * 32u; wb < len; wb += nwarps * 32u) {
+            const uint32_t idx = wb + lane;
+            uint32_t p = 0xFFFFFFFFu;
             if (idx < len) {
-                uint32_t p = dense ? idx : qcur[idx];
+                p = dense ? idx : qcur[idx];
                 if (swap) p ^= 1u;
-                if (p < a.P) {
-                    const uint32_t v = __ldg(&a.vowner[p]);
-                    const uint32_t d = __ldcg(&a.dist[v]);
-                    if (!unreached<OP>(d)) {
-                        ++my_parts;
-                        uint32_t col[K], wt[K];
-                        ld_part<K>(a.vcol + (size_t)p * K, col, pol);
-                        if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+            }
+            const bool valid = p < a.P;
+            uint32_t col[K], wt[K];
+            uint32_t d = 0;
+            bool active = false;
+            if (valid) {
+                const uint32_t v = __ldg(&a.vowner[p]);
+                if (!TD) {  // DD: the part is almost surely live -- fetch its row alongside the owner's value
+                    ld_part<K>(a.vcol + (size_t)p * K, col, pol);
+                    if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                }
+                d = __ldcg(&a.dist[v]);
+                active = !unreached<OP>(d);
+                if (TD && active) {
+                    ld_part<K>(a.vcol + (size_t)p * K, col, pol);
+                    if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                }
+                if (active) ++my_parts;
+            }
 #pragma unroll
-                        for (int i = 0; i < K; ++i) {
-                            const uint32_t t = col[i];
-                            if (t == NO_EDGE) break;
-                            ++my_edges;
-                            const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                            if (better<OP>(nd, __ldcg(&a.dist[t]))) {
-                                const uint32_t prev = atomic_improve<OP>(&a.dist[t], nd);
-                                if (better<OP>(nd, prev)) {
-                                    ++my_updates;
-                                    if (TD) {
-                                        changed = 1u;
-                                    } else if (__ldcg(&a.stamp[t]) != tag && atomicExch(&a.stamp[t], tag) != tag) {
-                                        const uint32_t pos = atomicAdd(&s_cnt, 1u);
-                                        if (pos < (uint32_t)ACT_CAP) {
-                                            s_act[pos] = t;
-                                        } else {  // CTA buffer full: append this vertex directly
-                                            const uint32_t s0 = a.vstart[t], np = a.vstart[t + 1] - s0;
-                                            const uint32_t b0 = np ? atomicAdd(&ctrl->qparts[nxt], np) : 0u;
-                                            atomicAdd(&ctrl->qverts[nxt], 1u);
-                                            for (uint32_t j = 0; j < np; ++j) qnext[b0 + j] = s0 + j;
-                                        }
-                                    }
-                                }
-                            }
+            for (int i = 0; i < K; ++i) {
+                bool claim = false;
+                uint32_t t = 0;
+                if (active && col[i] != NO_EDGE) {
+                    t = col[i];
+                    ++my_edges;
+                    const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
+                    if (better<OP>(nd, __ldcg(&a.dist[t]))) {
+                        const uint32_t prev = atomic_improve<OP>(&a.dist[t], nd);
+                        if (better<OP>(nd, prev)) {
+                            ++my_updates;
+                            if (TD) changed = 1u;
+                            else claim = __ldcg(&a.stamp[t]) != tag && atomicExch(&a.stamp[t], tag) != tag;
                         }
                     }
                 }
-            }
-            if (!TD) {
-                // ---- CTA-aggregated append of the claimed vertices' parts to the next queue
-                __syncthreads();
-                const uint32_t A = min(s_cnt, (uint32_t)ACT_CAP);
-                uint32_t mysum = 0;
-                for (uint32_t i = threadIdx.x; i < A; i += T_TPB) {
-                    const uint32_t t = s_act[i];
-                    mysum += a.vstart[t + 1] - a.vstart[t];
-                }
-                uint32_t total;
-                uint32_t off = block_exclusive_sum(mysum, s_warp, &total);
-                if (threadIdx.x == 0) {
-                    s_base = total ? atomicAdd(&ctrl->qparts[nxt], total) : 0u;
-                    if (A) atomicAdd(&ctrl->qverts[nxt], A);
-                    s_cnt = 0;
-                    s_nbig = 0;
-                }
-                __syncthreads();
-                uint32_t dstpos = s_base + off;
-                for (uint32_t i = threadIdx.x; i < A; i += T_TPB) {
-                    const uint32_t t = s_act[i];
-                    const uint32_t s0 = a.vstart[t], np = a.vstart[t + 1] - s0;
-                    if (np <= (uint32_t)BIG_PARTS) {
-                        for (uint32_t j = 0; j < np; ++j) qnext[dstpos + j] = s0 + j;
-                    } else {
-                        const uint32_t b = atomicAdd(&s_nbig, 1u);
-                        if (b < (uint32_t)BIG_CAP) s_big[b] = BigEntry{s0, np, dstpos};
-                        else
-                            for (uint32_t j = 0; j < np; ++j) qnext[dstpos + j] = s0 + j;
+                if (!TD) {
+                    const uint32_t mask = __ballot_sync(0xffffffffu, claim);
+                    if (mask) {
+                        const uint32_t c = __popc(mask);
+                        if (wcnt + c > (uint32_t)WCAP) {
+                            warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
+                            wcnt = 0;
+                        }
+                        if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
+                        wcnt += c;
                     }
-                    dstpos += np;
-                }
-                __syncthreads();
-                const uint32_t nb = min(s_nbig, (uint32_t)BIG_CAP);
-                for (uint32_t b = 0; b < nb; ++b) {
-                    const BigEntry e = s_big[b];
-                    for (uint32_t j = threadIdx.x; j < e.count; j += T_TPB) qnext[e.dst + j] = e.first + j;
                 }
             }
         }
         if (TD) {
             if (__syncthreads_or(changed) && threadIdx.x == 0) atomicAdd(&ctrl->qparts[nxt], 1u);
+        } else if (wcnt) {
+            warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
         }
         if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
     }
@@ -247,7 +266,7 @@ finish:
         my_edges += __shfl_down_sync(0xffffffffu, my_edges, off);
         my_updates += __shfl_down_sync(0xffffffffu, my_updates, off);
     }
-    if ((threadIdx.x & 31u) == 0) {
+    if (lane == 0) {
         if (my_parts) atomicAdd(&ctrl->parts_processed, my_parts);
         if (my_edges) atomicAdd(&ctrl->edges_scanned, my_edges);
         if (my_updates) atomicAdd(&ctrl->updates, my_updates);
