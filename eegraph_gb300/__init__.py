@@ -38,8 +38,9 @@ EXPORTED = [
     "eeg_graph_destroy", "eeg_graph_save_bcsr", "eeg_gen_rmat", "eeg_gen_grid", "eeg_symmetrize",
     "eeg_vgraph_build", "eeg_vgraph_build_arrays", "eeg_vgraph_get_info", "eeg_vgraph_download",
     "eeg_vgraph_export_reference_layout", "eeg_vgraph_destroy", "eeg_options_init", "eeg_run",
-    "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
+    "eeg_run_noalloc", "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
 ]
+NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
 class GraphView(C.Structure):
@@ -112,6 +113,8 @@ def _load() -> C.CDLL:
         "eeg_options_init": (None, [C.POINTER(Options)]),
         "eeg_run": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint32, C.POINTER(Options), vp, C.c_int, u32p, C.c_uint32,
                               vp, C.POINTER(Result)]),
+        "eeg_run_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_uint32, C.c_uint64, C.c_uint32, vp, vp, vp, vp,
+                                      C.c_uint32, vp, vp, C.POINTER(C.c_uint32)]),
         "eeg_energy_begin": (C.c_int, [C.c_int, C.c_char_p, C.c_uint32, C.POINTER(vp)]),
         "eeg_energy_mark": (C.c_int, [vp]),
         "eeg_energy_end": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),

@@ -232,6 +232,25 @@ EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, u
                            const eeg_options* opts, void* out, int out_on_device, uint32_t* activity,
                            uint32_t activity_cap, void* stream, eeg_result* res);
 
+/* Allocation-free traversal run. No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory when they run a query -- plugins whose host application owns all GPU memory,
+ * frameworks that route every allocation through their own pool, service loops where cudaMalloc's
+ * possible device synchronisation is not allowed. The caller passes the virtual graph (the layout of
+ * eeg_vgraph_download: vstart[n+1], vowner[P], vcol/vw[P*K]; vw may be NULL for BFS) and the output
+ * dist[n], all in device memory it owns; the working memory (control block, part queues, round stamps)
+ * lives in one fixed device array of EEG_NOALLOC_SCRATCH_BYTES that every GPU loading this library
+ * holds until the process exits. The call allocates nothing (no cudaMalloc/cudaFree, no allocating
+ * library routine). It rejects graphs whose working memory, 256 + 4*(2*P + n) bytes rounded up to
+ * 256-byte blocks, exceeds the array (EEG_ERR_INVALID). The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress) -- make that first call before any stream capture. All calls on a device
+ * share the array: calls that overlap on the GPU (unordered streams or threads) race and must be
+ * serialised by the caller. Results equal eeg_run's; *iterations (may be NULL) receives the rounds. */
+#define EEG_NOALLOC_SCRATCH_BYTES (32u << 20)
+EEG_API eeg_status eeg_run_noalloc(eeg_algo algo, eeg_variant variant, uint32_t num_nodes, uint64_t num_parts,
+                                   uint32_t K, const uint32_t* vstart, const uint32_t* vowner, const uint32_t* vcol,
+                                   const uint32_t* vw, uint32_t source, uint32_t* dist, void* stream,
+                                   uint32_t* iterations);
+
 /* ------------------------------------------------------------------ energy (NVML) */
 
 /* GPU energy over a region, from NVML's total-energy counter (mJ) with a power-sampling
