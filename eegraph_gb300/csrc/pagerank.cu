@@ -81,11 +81,35 @@ __device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, double sum
     cnext[v] = od ? xn / (float)od : 0.f;
 }
 
+constexpr int XCAP = 64;  // per-warp list of (vertex, chunks spanned) awaiting their arrival count
+
+// Count this warp's deliveries for the vertices in `xb` (their FP64 partials are already added): one
+// fence makes all of the warp's partials visible first; a lane whose increment completes a vertex's
+// count reads and clears the partial and finalises the vertex. Called by all 32 lanes, `nx` uniform.
+template <class Fin>
+__device__ __forceinline__ void settle_spanning(const PRArgs& a, const uint2* xb, uint32_t nx, uint32_t lane,
+                                                Fin&& fin) {
+    __syncwarp();
+    __threadfence();
+    for (uint32_t e = lane; e < nx; e += 32u) {
+        const uint2 q = xb[e];
+        if (atomicAdd(&a.arrive[q.x], 1u) + 1u == q.y) {
+            __threadfence();
+            const unsigned long long bits = atomicExch((unsigned long long*)&a.acc[q.x], 0ull);
+            a.arrive[q.x] = 0u;
+            fin(q.x, __longlong_as_double((long long)bits));
+        }
+    }
+    __syncwarp();
+}
+
 template <int K>
 __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
     constexpr int PR_U = InFlight<K>::U;
     __shared__ double s_red[2][PR_TPB / 32];
     __shared__ unsigned long long s_zero;
+    __shared__ uint2 s_span[PR_TPB / 32][XCAP];
+    uint2* xbuf = s_span[threadIdx.x >> 5];
     PRCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * PR_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * PR_TPB;
@@ -130,9 +154,15 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
                 ctrl->resid[(s + 1u) % 3u] = 0.0;
                 ctrl->norm[(s + 1u) % 3u] = 0.0;
             }
-            const float* __restrict__ ccur = (s & 1u) && !a.inplace ? a.c1 : a.c0;
+            // ccur is read through L1 (plain loads): the grid barrier's acquire makes the previous sweep's
+            // values visible, and within a sweep they do not change (SYNC) or may be stale (ASYNC, allowed)
+            const float* ccur = (s & 1u) && !a.inplace ? a.c1 : a.c0;
             float* cnext = a.inplace ? a.c0 : ((s & 1u) ? a.c0 : a.c1);
             double r = 0.0, nrm = 0.0;
+            uint32_t nx = 0;  // warp-uniform fill of xbuf
+            auto fin = [&](uint32_t vv, double sum) {
+                finalize(a, vv, sum, __ldcg(&a.x[vv]), __ldg(&a.outdeg[vv]), cnext, r, nrm);
+            };
 
             for (uint32_t base = gwarp; base < nchunks; base += nwarps * PR_U) {
                 uint32_t v[PR_U], col[PR_U][K];
@@ -153,7 +183,7 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
                 for (int u = 0; u < PR_U; ++u)
 #pragma unroll
                     for (int i = 0; i < K; ++i)
-                        y[u][i] = (valid[u] && col[u][i] != NO_EDGE) ? __ldcg(&ccur[col[u][i]]) : 0.f;
+                        y[u][i] = (valid[u] && col[u][i] != NO_EDGE) ? ccur[col[u][i]] : 0.f;
                 // segment ends: prefetch what finalisation needs while the gathers are in flight
                 bool last[PR_U];
                 float xo[PR_U];
@@ -192,27 +222,32 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
                         const float lo2 = __shfl_up_sync(0xffffffffu, lo, off);
                         if (lane >= (uint32_t)off && vo == v[u]) pair_add(hi, lo, ho, lo2);
                     }
+                    bool spans = false;
+                    uint32_t need = 0;
                     if (last[u]) {
                         const uint32_t ch = base + (uint32_t)u * nwarps;
                         const uint32_t first_chunk = vs0[u] / 32u, last_chunk = (vs1[u] - 1u) / 32u;
                         if (first_chunk == ch && last_chunk == ch) {
                             finalize(a, v[u], (double)hi + (double)lo, xo[u], od[u], cnext, r, nrm);
-                        } else {
+                        } else {  // partial now, arrival counted in the warp's next settle
                             atomicAdd(&a.acc[v[u]], (double)hi + (double)lo);
-                            __threadfence();
-                            const uint32_t need = last_chunk - first_chunk + 1u;
-                            if (atomicAdd(&a.arrive[v[u]], 1u) + 1u == need) {
-                                __threadfence();
-                                const unsigned long long bits =
-                                    atomicExch((unsigned long long*)&a.acc[v[u]], 0ull);
-                                a.arrive[v[u]] = 0u;
-                                finalize(a, v[u], __longlong_as_double((long long)bits), xo[u], od[u], cnext, r,
-                                         nrm);
-                            }
+                            spans = true;
+                            need = last_chunk - first_chunk + 1u;
                         }
+                    }
+                    const uint32_t m = __ballot_sync(0xffffffffu, spans);
+                    if (m) {
+                        const uint32_t c = __popc(m);
+                        if (nx + c > (uint32_t)XCAP) {
+                            settle_spanning(a, xbuf, nx, lane, fin);
+                            nx = 0;
+                        }
+                        if (spans) xbuf[nx + __popc(m & ((1u << lane) - 1u))] = make_uint2(v[u], need);
+                        nx += c;
                     }
                 }
             }
+            if (nx) settle_spanning(a, xbuf, nx, lane, fin);
             // CTA reduction of the FP64 residual / norm, one atomic per CTA
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1) {

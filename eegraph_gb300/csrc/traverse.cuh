@@ -188,8 +188,9 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             ctrl->qparts[old] = 0u;
             ctrl->qverts[old] = 0u;
         }
-        const uint32_t* __restrict__ qcur = (it & 1u) ? a.q1 : a.q0;
-        uint32_t* __restrict__ qnext = (it & 1u) ? a.q0 : a.q1;
+        // no __restrict__/const-qualified read-only path here: each queue is rewritten every other round
+        const uint32_t* qcur = (it & 1u) ? a.q1 : a.q0;
+        uint32_t* qnext = (it & 1u) ? a.q0 : a.q1;
         const uint32_t tag = it + 1u;
         uint32_t changed = 0;
         uint32_t wcnt = 0;  // warp-uniform fill of wbuf
@@ -211,7 +212,9 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                     ld_part<K>(a.vcol + (size_t)p * K, col, pol);
                     if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
                 }
-                d = __ldcg(&a.dist[v]);
+                // plain (L1-cached) value reads: the grid barrier's acquire makes the previous round's
+                // values visible; a value improved later in this round re-enqueues its vertex anyway
+                d = a.dist[v];
                 active = !unreached<OP>(d);
                 if (TD && active) {
                     ld_part<K>(a.vcol + (size_t)p * K, col, pol);
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                     t = col[i];
                     ++my_edges;
                     const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                    if (better<OP>(nd, __ldcg(&a.dist[t]))) {
+                    if (better<OP>(nd, a.dist[t])) {  // filter; a stale (larger) value only costs an atomic
                         const uint32_t prev = atomic_improve<OP>(&a.dist[t], nd);
                         if (better<OP>(nd, prev)) {
                             ++my_updates;
