@@ -214,13 +214,16 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
                         hi = t;
                         lo = __fadd_rn(lo, e);
                     }
-                    // segmented inclusive scan over lanes of the same vertex (a vertex's parts are contiguous)
-#pragma unroll
-                    for (int off = 1; off < 32; off <<= 1) {
-                        const uint32_t vo = __shfl_up_sync(0xffffffffu, v[u], off);
+                    // segmented inclusive scan over lanes of the same vertex (a vertex's parts are contiguous):
+                    // segment heads from one shuffle + ballot, and only as many steps as the longest segment
+                    const uint32_t vprev = __shfl_up_sync(0xffffffffu, v[u], 1);
+                    const uint32_t heads = __ballot_sync(0xffffffffu, lane == 0u || vprev != v[u]);
+                    const uint32_t seg0 = 31u - __clz(heads & (0xffffffffu >> (31u - lane)));
+                    const uint32_t span = __reduce_max_sync(0xffffffffu, lane - seg0 + 1u);
+                    for (uint32_t off = 1; off < span; off <<= 1) {
                         const float ho = __shfl_up_sync(0xffffffffu, hi, off);
                         const float lo2 = __shfl_up_sync(0xffffffffu, lo, off);
-                        if (lane >= (uint32_t)off && vo == v[u]) pair_add(hi, lo, ho, lo2);
+                        if (lane >= seg0 + off) pair_add(hi, lo, ho, lo2);
                     }
                     bool spans = false;
                     uint32_t need = 0;
