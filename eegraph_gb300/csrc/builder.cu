@@ -4,15 +4,16 @@
 // UM twin src/um_virtual_graph.cu:36-111), which build an interleaved host array on one core and
 // drop every edge whose slot index reaches num_edges (src/virtual_graph.cpp:86-88). Here:
 //
-//   1. degree histogram            deg[s]++ for every edge (atomics in L2)
-//   2. part counts                 np[v] = ceil(deg[v] / K)
-//   3. exclusive scan              vstart[v] = sum_{u<v} np[u]; vstart[n] = P (numParts)
+//   1. stable radix sort           (owner, neighbour[, weight]) by owner, 8-bit digits (no hot atomics:
+//                                  a hub's edges are ranked inside each 4096-key tile)
+//   2. runs                        first/last index of each owner -> degree
+//   3. part counts + scan          np[v] = ceil(deg[v] / K); vstart = exclusive scan; vstart[n] = P
 //   4. owner table (segmented)     vowner[vstart[v]] = v for v with parts, then inclusive max-scan
-//   5. scatter                     edge r of vertex s -> slot vstart[s]*K + r (part r/K, lane r%K)
+//   5. placement                   sorted edge of rank r of vertex s -> slot vstart[s]*K + r (part r/K)
 //
-// The result is lossless. Part p of vertex v holds out-edges [ (p - vstart[v]) * K, +K ) of v in one
-// K-slot row, so a thread reads a whole part with K/4 aligned 128-bit loads. Edges keep the order of
-// the atomic rank within a vertex; fixed points do not depend on it.
+// The result is lossless and deterministic. Part p of vertex v holds out-edges [ (p - vstart[v]) * K,
+// +K ) of v in one K-slot row, in input order (the order MakeGraph gives them), so a thread reads a
+// whole part with one or two aligned 256-bit loads.
 #include <algorithm>
 #include <cstdio>
 
@@ -139,29 +140,119 @@ eeg_status device_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, bool i
 namespace {
 
 constexpr int B_TPB = 256;
+// stable LSD radix sort of (owner, neighbour[, weight]) by owner: 8-bit digits, tiles of 4096 keys
+constexpr int R_TPB = 256;
+constexpr int R_ITEMS = 16;
+constexpr int R_TILE = R_TPB * R_ITEMS;
+constexpr int R_BINS = 256;
+static_assert(R_TPB == R_BINS, "one thread per digit in the cross-warp prefix");
 
-__global__ void k_degree(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst, uint64_t m, uint32_t n,
-                         uint32_t shift, uint32_t* __restrict__ deg, uint32_t* __restrict__ err) {
+// 0-based owner/neighbour (+ weight) into the sort buffers; endpoints outside [0, n) raise err.
+__global__ void k_prepare(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, const uint32_t* __restrict__ w,
+                          uint64_t m, uint32_t n, uint32_t shift, uint32_t* __restrict__ key, uint32_t* __restrict__ nb,
+                          uint32_t* __restrict__ wt, uint32_t* __restrict__ err) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t s = src[e] - shift, t = dst[e] - shift;
+        uint32_t s = a[e] - shift, t = b[e] - shift;
         if (s >= n || t >= n) {
             atomicOr(err, 1u);
-            continue;
+            s = 0;
+            t = 0;
         }
-        atomicAdd(&deg[s], 1u);
+        key[e] = s;
+        nb[e] = t;
+        if (wt) wt[e] = w ? w[e] : 1u;
     }
 }
 
-// np[v] = ceil(deg/K) for v < n, np[n] = 0; also the max-degree vertex (lowest id among ties).
-__global__ void k_nparts(const uint32_t* __restrict__ deg, uint32_t n, uint32_t K, uint32_t* __restrict__ np,
-                         unsigned long long* __restrict__ best) {
+// digit counts of one tile, stored digit-major: hist[digit * ntiles + tile]
+__global__ void __launch_bounds__(R_TPB) k_radix_hist(const uint32_t* __restrict__ key, uint64_t m, uint32_t shift,
+                                                      uint32_t* __restrict__ hist, uint32_t ntiles) {
+    __shared__ uint32_t h[R_BINS];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * R_TILE;
+#pragma unroll 4
+    for (int j = 0; j < R_ITEMS; ++j) {
+        const uint64_t idx = base + (uint64_t)j * R_TPB + threadIdx.x;
+        if (idx < m) atomicAdd(&h[(key[idx] >> shift) & (R_BINS - 1)], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile by digit. Keys of the tile are taken in index order (round j, warp, lane);
+// a key's place = the tile's global offset for its digit + keys with that digit earlier in the tile.
+__global__ void __launch_bounds__(R_TPB) k_radix_scatter(const uint32_t* __restrict__ key_in,
+                                                         const uint32_t* __restrict__ nb_in,
+                                                         const uint32_t* __restrict__ w_in, uint32_t* __restrict__ key_out,
+                                                         uint32_t* __restrict__ nb_out, uint32_t* __restrict__ w_out,
+                                                         uint64_t m, uint32_t shift, const uint32_t* __restrict__ offs,
+                                                         uint32_t ntiles) {
+    __shared__ uint32_t s_off[R_BINS];
+    __shared__ uint32_t s_cnt[R_TPB / 32][R_BINS];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    s_off[threadIdx.x] = offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    const uint64_t base = (uint64_t)blockIdx.x * R_TILE;
+    for (int j = 0; j < R_ITEMS; ++j) {
+        const uint64_t idx = base + (uint64_t)j * R_TPB + threadIdx.x;
+        const bool valid = idx < m;
+        uint32_t k = 0, v = 0, wv = 0;
+        if (valid) {
+            k = key_in[idx];
+            v = nb_in[idx];
+            if (w_out) wv = w_in[idx];
+        }
+        const uint32_t digit = valid ? (k >> shift) & (R_BINS - 1) : (uint32_t)R_BINS;
+#pragma unroll
+        for (int w = 0; w < R_TPB / 32; ++w) s_cnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        const uint32_t rk = __popc(peers & ((1u << lane) - 1u));
+        if (valid && rk == 0) s_cnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        {  // exclusive prefix over warps for digit = threadIdx.x, continuing the tile's running offset
+            uint32_t run = s_off[threadIdx.x];
+#pragma unroll
+            for (int w = 0; w < R_TPB / 32; ++w) {
+                const uint32_t c = s_cnt[w][threadIdx.x];
+                s_cnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            s_off[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = s_cnt[warp][digit] + rk;
+            key_out[pos] = k;
+            nb_out[pos] = v;
+            if (w_out) w_out[pos] = wv;
+        }
+        __syncthreads();
+    }
+}
+
+// first and one-past-last index of every owner's run in the sorted keys
+__global__ void k_runs(const uint32_t* __restrict__ key, uint64_t m, uint32_t* __restrict__ rs,
+                       uint32_t* __restrict__ re) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t o = key[i];
+        if (i == 0 || key[i - 1] != o) rs[o] = (uint32_t)i;
+        if (i + 1 == m || key[i + 1] != o) re[o] = (uint32_t)(i + 1);
+    }
+}
+
+// deg[v] = run length; np[v] = ceil(deg/K) for v < n, np[n] = 0; also the max-degree vertex
+// (lowest id among ties).
+__global__ void k_nparts(const uint32_t* __restrict__ rs, const uint32_t* __restrict__ re, uint32_t n, uint32_t K,
+                         uint32_t* __restrict__ deg, uint32_t* __restrict__ np, unsigned long long* __restrict__ best) {
     unsigned long long mine = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v <= n; v += gridDim.x * blockDim.x) {
         if (v == n) {
             np[v] = 0;
             continue;
         }
-        uint32_t d = deg[v];
+        const uint32_t d = re[v] - rs[v];
+        deg[v] = d;
         np[v] = (d + K - 1) / K;
         unsigned long long key = ((unsigned long long)d << 32) | (unsigned long long)(0xFFFFFFFFu - v);
         mine = key > mine ? key : mine;
@@ -181,16 +272,15 @@ __global__ void k_heads(const uint32_t* __restrict__ vstart, uint32_t n, uint32_
     }
 }
 
-__global__ void k_scatter(const uint32_t* __restrict__ src, const uint32_t* __restrict__ dst,
-                          const uint32_t* __restrict__ w, uint64_t m, uint32_t shift, uint32_t K,
-                          const uint32_t* __restrict__ vstart, uint32_t* __restrict__ cursor,
-                          uint32_t* __restrict__ vcol, uint32_t* __restrict__ vw) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t s = src[e] - shift, t = dst[e] - shift;
-        uint32_t r = atomicAdd(&cursor[s], 1u);
-        size_t slot = (size_t)vstart[s] * K + r;
-        vcol[slot] = t;
-        if (vw) vw[slot] = w ? w[e] : 1u;
+// sorted edge i of owner o (rank r = i - rs[o]) goes to slot vstart[o]*K + r: part r/K, lane r%K
+__global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __restrict__ nb, const uint32_t* __restrict__ wt,
+                        uint64_t m, uint32_t K, const uint32_t* __restrict__ rs, const uint32_t* __restrict__ vstart,
+                        uint32_t* __restrict__ vcol, uint32_t* __restrict__ vw) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t o = key[i];
+        const size_t slot = (size_t)vstart[o] * K + (i - rs[o]);
+        vcol[slot] = nb[i];
+        if (vw) vw[slot] = wt ? wt[i] : 1u;
     }
 }
 
@@ -210,7 +300,32 @@ static unsigned grid_for(uint64_t work, int device) {
     return (unsigned)blocks;
 }
 
+namespace {
+// stream-ordered temporaries released on every exit path
+struct TempSet {
+    cudaStream_t st;
+    void* p[16] = {nullptr};
+    int k = 0;
+    explicit TempSet(cudaStream_t s) : st(s) {}
+    eeg_status get(void** out, size_t bytes) {
+        if (k == 16) {
+            set_last_error("builder: too many temporaries");
+            return EEG_ERR_INVALID;
+        }
+        cudaError_t e = cudaMallocAsync(out, bytes ? bytes : 4, st);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(builder temporaries)", __FILE__, __LINE__);
+        p[k++] = *out;
+        return EEG_OK;
+    }
+    ~TempSet() {
+        for (int i = 0; i < k; ++i) cudaFreeAsync(p[i], st);
+    }
+};
+}  // namespace
+
 // Build one direction. reverse: edges (s,t) are inserted as (t,s) -- the transposed graph.
+// Edges are sorted by owner with a stable radix sort, so each vertex's edges keep the input order
+// (the order the reference's MakeGraph gives them) and the layout is deterministic.
 eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst,
                            const uint32_t* d_w, bool reverse, cudaStream_t st) {
     const uint32_t n = vg->n, K = vg->K;
@@ -218,23 +333,47 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     const uint32_t shift = (vg->flags & EEG_VG_SHIFT_ONE) ? 1u : 0u;
     const uint32_t* a = reverse ? d_dst : d_src;
     const uint32_t* b = reverse ? d_src : d_dst;
+    const bool with_w = (d_w != nullptr) || (!reverse && vg->weighted);
 
     EEG_TRY(vg_alloc(vg, (void**)&d->deg, sizeof(uint32_t) * (size_t)(n + 1)));
     EEG_TRY(vg_alloc(vg, (void**)&d->vstart, sizeof(uint32_t) * (size_t)(n + 1)));
-    uint32_t* np = nullptr;
-    uint32_t* tmp = nullptr;
-    uint32_t* err = nullptr;
-    unsigned long long* best = nullptr;
-    const uint64_t tmpw = device_scan_tmp_words(std::max<uint64_t>(n + 1, 1));
-    EEG_CUDA(cudaMallocAsync((void**)&np, sizeof(uint32_t) * (size_t)(n + 1), st));
-    EEG_CUDA(cudaMallocAsync((void**)&tmp, sizeof(uint32_t) * (size_t)tmpw, st));
-    EEG_CUDA(cudaMallocAsync((void**)&err, 16, st));
-    best = (unsigned long long*)(err + 2);
+    TempSet T(st);
+    uint32_t *key[2] = {nullptr, nullptr}, *nb[2] = {nullptr, nullptr}, *wt[2] = {nullptr, nullptr};
+    uint32_t *rs = nullptr, *re = nullptr, *np = nullptr, *tmp = nullptr, *err = nullptr, *hist = nullptr;
+    for (int i = 0; i < 2; ++i) {
+        EEG_TRY(T.get((void**)&key[i], sizeof(uint32_t) * m));
+        EEG_TRY(T.get((void**)&nb[i], sizeof(uint32_t) * m));
+        if (with_w) EEG_TRY(T.get((void**)&wt[i], sizeof(uint32_t) * m));
+    }
+    EEG_TRY(T.get((void**)&rs, sizeof(uint32_t) * (size_t)(n + 1)));
+    EEG_TRY(T.get((void**)&re, sizeof(uint32_t) * (size_t)(n + 1)));
+    EEG_TRY(T.get((void**)&np, sizeof(uint32_t) * (size_t)(n + 1)));
+    EEG_TRY(T.get((void**)&err, 16));
+    unsigned long long* best = (unsigned long long*)(err + 2);
+    const uint64_t ntiles = (m + R_TILE - 1) / R_TILE;
+    const uint64_t hwords = std::max<uint64_t>(ntiles * R_BINS, 1);
+    EEG_TRY(T.get((void**)&hist, sizeof(uint32_t) * hwords));
+    EEG_TRY(T.get((void**)&tmp, sizeof(uint32_t) * device_scan_tmp_words(std::max<uint64_t>(hwords, (uint64_t)n + 1))));
     EEG_CUDA(cudaMemsetAsync(err, 0, 16, st));
-    EEG_CUDA(cudaMemsetAsync(d->deg, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
+    EEG_CUDA(cudaMemsetAsync(rs, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
+    EEG_CUDA(cudaMemsetAsync(re, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
 
-    k_degree<<<grid_for(m, vg->device), B_TPB, 0, st>>>(a, b, m, n, shift, d->deg, err);
-    k_nparts<<<grid_for((uint64_t)n + 1, vg->device), B_TPB, 0, st>>>(d->deg, n, K, np, best);
+    int cur = 0;
+    if (m > 0) {
+        k_prepare<<<grid_for(m, vg->device), B_TPB, 0, st>>>(a, b, with_w ? d_w : nullptr, m, n, shift, key[0], nb[0],
+                                                              with_w ? wt[0] : nullptr, err);
+        const uint32_t bits = n > 1 ? 32u - (uint32_t)__builtin_clz(n - 1) : 1u;
+        for (uint32_t sh = 0; sh < bits; sh += 8) {
+            k_radix_hist<<<(unsigned)ntiles, R_TPB, 0, st>>>(key[cur], m, sh, hist, (uint32_t)ntiles);
+            EEG_TRY(device_scan_u32(hist, hist, ntiles * R_BINS, false, SCAN_ADD, tmp, st));
+            k_radix_scatter<<<(unsigned)ntiles, R_TPB, 0, st>>>(key[cur], nb[cur], wt[cur], key[cur ^ 1], nb[cur ^ 1],
+                                                                with_w ? wt[cur ^ 1] : nullptr, m, sh, hist,
+                                                                (uint32_t)ntiles);
+            cur ^= 1;
+        }
+        k_runs<<<grid_for(m, vg->device), B_TPB, 0, st>>>(key[cur], m, rs, re);
+    }
+    k_nparts<<<grid_for((uint64_t)n + 1, vg->device), B_TPB, 0, st>>>(rs, re, n, K, d->deg, np, best);
     EEG_TRY(device_scan_u32(np, d->vstart, (uint64_t)n + 1, false, SCAN_ADD, tmp, st));
 
     uint32_t hbuf[4] = {0, 0, 0, 0};
@@ -243,23 +382,19 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     EEG_CUDA(cudaMemcpyAsync(&P32, d->vstart + n, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     EEG_CUDA(cudaStreamSynchronize(st));
     if (hbuf[0]) {
-        cudaFreeAsync(np, st);
-        cudaFreeAsync(tmp, st);
-        cudaFreeAsync(err, st);
         set_last_error("edge endpoint outside [0, num_nodes)");
         return EEG_ERR_INVALID;
     }
     if (!reverse) {
-        unsigned long long key = ((unsigned long long)hbuf[3] << 32) | hbuf[2];
-        vg->max_deg = (uint32_t)(key >> 32);
-        vg->max_deg_vertex = key ? 0xFFFFFFFFu - (uint32_t)(key & 0xFFFFFFFFu) : 0u;
+        unsigned long long kbest = ((unsigned long long)hbuf[3] << 32) | hbuf[2];
+        vg->max_deg = (uint32_t)(kbest >> 32);
+        vg->max_deg_vertex = kbest ? 0xFFFFFFFFu - (uint32_t)(kbest & 0xFFFFFFFFu) : 0u;
     }
     const uint64_t P = P32;
     d->P = P;
     const size_t slots = (size_t)P * K;
     EEG_TRY(vg_alloc(vg, (void**)&d->vowner, sizeof(uint32_t) * (size_t)std::max<uint64_t>(P, 1)));
     EEG_TRY(vg_alloc(vg, (void**)&d->vcol, sizeof(uint32_t) * std::max<size_t>(slots, 4)));
-    const bool with_w = (d_w != nullptr) || (!reverse && vg->weighted);
     if (with_w) EEG_TRY(vg_alloc(vg, (void**)&d->vw, sizeof(uint32_t) * std::max<size_t>(slots, 4)));
 
     if (P > 0) {
@@ -268,17 +403,12 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
         if (d->vw) EEG_CUDA(cudaMemsetAsync(d->vw, 0, sizeof(uint32_t) * slots, st));
         k_heads<<<grid_for(n, vg->device), B_TPB, 0, st>>>(d->vstart, n, d->vowner);
         uint32_t* tmp2 = nullptr;
-        EEG_CUDA(cudaMallocAsync((void**)&tmp2, sizeof(uint32_t) * (size_t)device_scan_tmp_words(P), st));
+        EEG_TRY(T.get((void**)&tmp2, sizeof(uint32_t) * (size_t)device_scan_tmp_words(P)));
         EEG_TRY(device_scan_u32(d->vowner, d->vowner, P, true, SCAN_MAX, tmp2, st));
-        EEG_CUDA(cudaFreeAsync(tmp2, st));
-        // cursor reuses np (n+1 words)
-        EEG_CUDA(cudaMemsetAsync(np, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
-        k_scatter<<<grid_for(m, vg->device), B_TPB, 0, st>>>(a, b, d_w, m, shift, K, d->vstart, np, d->vcol, d->vw);
+        k_place<<<grid_for(m, vg->device), B_TPB, 0, st>>>(key[cur], nb[cur], with_w ? wt[cur] : nullptr, m, K, rs,
+                                                            d->vstart, d->vcol, d->vw);
     }
     EEG_CUDA(cudaGetLastError());
-    EEG_CUDA(cudaFreeAsync(np, st));
-    EEG_CUDA(cudaFreeAsync(tmp, st));
-    EEG_CUDA(cudaFreeAsync(err, st));
     vg->bytes += sizeof(uint32_t) * ((size_t)(n + 1) * 2 + (size_t)P + slots * (with_w ? 2 : 1));
     return EEG_OK;
 }
