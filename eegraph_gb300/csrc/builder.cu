@@ -5,7 +5,7 @@
 // drop every edge whose slot index reaches num_edges (src/virtual_graph.cpp:86-88). Here:
 //
 //   1. stable radix sort           (owner, neighbour[, weight]) by owner, 8-bit digits (no hot atomics:
-//                                  a hub's edges are ranked inside each 4096-key tile)
+//                                  a hub's edges are ranked inside each 2048-key tile)
 //   2. runs                        first/last index of each owner -> degree
 //   3. part counts + scan          np[v] = ceil(deg[v] / K); vstart = exclusive scan; vstart[n] = P
 //   4. owner table (segmented)     vowner[vstart[v]] = v for v with parts, then inclusive max-scan
@@ -140,9 +140,11 @@ eeg_status device_scan_u32(const uint32_t* in, uint32_t* out, uint64_t n, bool i
 namespace {
 
 constexpr int B_TPB = 256;
-// stable LSD radix sort of (owner, neighbour[, weight]) by owner: 8-bit digits, tiles of 4096 keys
+// stable LSD radix sort of (owner, neighbour[, weight]) by owner: 8-bit digits, tiles of 2048 keys;
+// warp w of a tile owns keys [w*256, w*256+256) of it and takes them 32 at a time, in order.
 constexpr int R_TPB = 256;
-constexpr int R_ITEMS = 16;
+constexpr int R_WARPS = R_TPB / 32;
+constexpr int R_ITEMS = 8;  // rounds of 32 keys per warp
 constexpr int R_TILE = R_TPB * R_ITEMS;
 constexpr int R_BINS = 256;
 static_assert(R_TPB == R_BINS, "one thread per digit in the cross-warp prefix");
@@ -171,63 +173,93 @@ __global__ void __launch_bounds__(R_TPB) k_radix_hist(const uint32_t* __restrict
     h[threadIdx.x] = 0;
     __syncthreads();
     const uint64_t base = (uint64_t)blockIdx.x * R_TILE;
-#pragma unroll 4
+    uint32_t k[R_ITEMS];
+#pragma unroll
     for (int j = 0; j < R_ITEMS; ++j) {
         const uint64_t idx = base + (uint64_t)j * R_TPB + threadIdx.x;
-        if (idx < m) atomicAdd(&h[(key[idx] >> shift) & (R_BINS - 1)], 1u);
+        k[j] = idx < m ? key[idx] : 0xFFFFFFFFu;
+    }
+#pragma unroll
+    for (int j = 0; j < R_ITEMS; ++j) {
+        const uint64_t idx = base + (uint64_t)j * R_TPB + threadIdx.x;
+        if (idx < m) atomicAdd(&h[(k[j] >> shift) & (R_BINS - 1)], 1u);
     }
     __syncthreads();
     hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Stable scatter of one tile by digit. Keys of the tile are taken in index order (round j, warp, lane);
-// a key's place = the tile's global offset for its digit + keys with that digit earlier in the tile.
+// Stable scatter of one tile by digit: a key's place = the tile's global offset for its digit + the keys
+// with that digit earlier in the tile (earlier warps, earlier rounds of its warp, lower lanes).
 __global__ void __launch_bounds__(R_TPB) k_radix_scatter(const uint32_t* __restrict__ key_in,
                                                          const uint32_t* __restrict__ nb_in,
                                                          const uint32_t* __restrict__ w_in, uint32_t* __restrict__ key_out,
                                                          uint32_t* __restrict__ nb_out, uint32_t* __restrict__ w_out,
                                                          uint64_t m, uint32_t shift, const uint32_t* __restrict__ offs,
                                                          uint32_t ntiles) {
-    __shared__ uint32_t s_off[R_BINS];
-    __shared__ uint32_t s_cnt[R_TPB / 32][R_BINS];
+    __shared__ uint32_t s_cnt[R_WARPS][R_BINS];
+    __shared__ uint32_t s_key[R_TILE], s_nb[R_TILE], s_w[R_TILE];
+    __shared__ uint32_t s_dstart[R_BINS], s_goff[R_BINS], s_warp[33];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    s_off[threadIdx.x] = offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
-    const uint64_t base = (uint64_t)blockIdx.x * R_TILE;
-    for (int j = 0; j < R_ITEMS; ++j) {
-        const uint64_t idx = base + (uint64_t)j * R_TPB + threadIdx.x;
-        const bool valid = idx < m;
-        uint32_t k = 0, v = 0, wv = 0;
-        if (valid) {
-            k = key_in[idx];
-            v = nb_in[idx];
-            if (w_out) wv = w_in[idx];
-        }
-        const uint32_t digit = valid ? (k >> shift) & (R_BINS - 1) : (uint32_t)R_BINS;
+    const uint64_t wbase = (uint64_t)blockIdx.x * R_TILE + (uint64_t)warp * (32 * R_ITEMS);
 #pragma unroll
-        for (int w = 0; w < R_TPB / 32; ++w) s_cnt[w][threadIdx.x] = 0;
-        __syncthreads();
+    for (int w = 0; w < R_WARPS; ++w) s_cnt[w][threadIdx.x] = 0;
+    uint32_t k[R_ITEMS], v[R_ITEMS], wv[R_ITEMS], rank[R_ITEMS];
+#pragma unroll
+    for (int j = 0; j < R_ITEMS; ++j) {  // all loads first (coalesced: 32 consecutive keys per round)
+        const uint64_t idx = wbase + (uint64_t)j * 32 + lane;
+        const bool valid = idx < m;
+        k[j] = valid ? key_in[idx] : 0u;
+        v[j] = valid ? nb_in[idx] : 0u;
+        wv[j] = (valid && w_out) ? w_in[idx] : 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < R_ITEMS; ++j) {
+        const uint64_t idx = wbase + (uint64_t)j * 32 + lane;
+        const uint32_t digit = idx < m ? (k[j] >> shift) & (R_BINS - 1) : (uint32_t)R_BINS;
         const uint32_t peers = __match_any_sync(0xffffffffu, digit);
         const uint32_t rk = __popc(peers & ((1u << lane) - 1u));
-        if (valid && rk == 0) s_cnt[warp][digit] = __popc(peers);
-        __syncthreads();
-        {  // exclusive prefix over warps for digit = threadIdx.x, continuing the tile's running offset
-            uint32_t run = s_off[threadIdx.x];
+        const uint32_t before = digit < R_BINS ? s_cnt[warp][digit] : 0u;
+        __syncwarp();
+        if (digit < R_BINS && rk == 0) s_cnt[warp][digit] = before + __popc(peers);
+        __syncwarp();
+        rank[j] = before + rk;
+    }
+    __syncthreads();
+    // per digit (thread = digit): offsets of each warp's keys inside the digit's run, and the run length
+    uint32_t cnt = 0;
 #pragma unroll
-            for (int w = 0; w < R_TPB / 32; ++w) {
-                const uint32_t c = s_cnt[w][threadIdx.x];
-                s_cnt[w][threadIdx.x] = run;
-                run += c;
-            }
-            s_off[threadIdx.x] = run;
+    for (int w = 0; w < R_WARPS; ++w) {
+        const uint32_t c = s_cnt[w][threadIdx.x];
+        s_cnt[w][threadIdx.x] = cnt;
+        cnt += c;
+    }
+    // the tile in digit order in shared memory: digit runs start at the exclusive scan of the counts
+    uint32_t total;
+    const uint32_t dstart = block_exclusive_sum(cnt, s_warp, &total);
+    s_dstart[threadIdx.x] = dstart;
+    s_goff[threadIdx.x] = offs[(size_t)threadIdx.x * ntiles + blockIdx.x];
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < R_ITEMS; ++j) {
+        const uint64_t idx = wbase + (uint64_t)j * 32 + lane;
+        if (idx < m) {
+            const uint32_t d = (k[j] >> shift) & (R_BINS - 1);
+            const uint32_t lp = s_dstart[d] + s_cnt[warp][d] + rank[j];
+            s_key[lp] = k[j];
+            s_nb[lp] = v[j];
+            if (w_out) s_w[lp] = wv[j];
         }
-        __syncthreads();
-        if (valid) {
-            const uint32_t pos = s_cnt[warp][digit] + rk;
-            key_out[pos] = k;
-            nb_out[pos] = v;
-            if (w_out) w_out[pos] = wv;
-        }
-        __syncthreads();
+    }
+    __syncthreads();
+    // write the digit runs out: consecutive threads -> consecutive addresses inside each run
+    for (uint32_t i = threadIdx.x; i < total; i += R_TPB) {
+        const uint32_t kk = s_key[i];
+        const uint32_t d = (kk >> shift) & (R_BINS - 1);
+        const uint32_t gp = s_goff[d] + (i - s_dstart[d]);
+        key_out[gp] = kk;
+        nb_out[gp] = s_nb[i];
+        if (w_out) w_out[gp] = s_w[i];
     }
 }
 

@@ -186,8 +186,32 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
     const uint32_t *ds = src, *dd = dst, *dw = w;
     uint32_t* tmp = nullptr;
     eeg_status s = EEG_OK;
+    // page-locked host arrays are read by the first build kernel in place (over NVLink-C2C / PCIe),
+    // which saves a copy into device temporaries
+    auto mapped = [](const uint32_t* p, const uint32_t** out) -> bool {
+        if (!p) {
+            *out = nullptr;
+            return true;
+        }
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return false;
+        }
+        if (at.type == cudaMemoryTypeHost && at.devicePointer) {
+            *out = (const uint32_t*)at.devicePointer;
+            return true;
+        }
+        return false;
+    };
+    const uint32_t *ms = nullptr, *md = nullptr, *mw = nullptr;
+    const bool zero_copy = !on_device && m > 0 && mapped(src, &ms) && mapped(dst, &md) && mapped(w, &mw);
     cudaEventRecord(e0, st);
-    if (!on_device && m > 0) {
+    if (zero_copy) {
+        ds = ms;
+        dd = md;
+        dw = mw;
+    } else if (!on_device && m > 0) {
         const size_t words = (size_t)m * (w ? 3 : 2);
         cudaError_t ce = cudaMallocAsync((void**)&tmp, words * sizeof(uint32_t), st);
         if (ce != cudaSuccess) {
