@@ -227,3 +227,20 @@ def test_repeated_runs_reuse_workspace(gpu):
             assert np.array_equal(got, oracle.dijkstra(n, s, d, w, src))
             got, _ = vg.run("bfs", "async_push_dd", src)
             assert np.array_equal(got, oracle.bfs(n, s, d, src))
+
+
+def test_build_from_page_locked_host_arrays(gpu):
+    """Page-locked inputs are read in place by the builder; the result equals the copied-input build."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 12
+    s, d, w = gpu.gen_rmat(12, 16, seed=13, wmin=1, wmax=63)
+    pin = [torch.from_numpy(a.view(np.int32)).pin_memory().numpy().view(np.uint32) for a in (s, d, w)]
+    with gpu.VirtualGraph.build(n, *pin, K=8, reverse=True) as vg_pin, gpu.VirtualGraph.build(n, s, d, w, K=8,
+                                                                                              reverse=True) as vg:
+        a, b = vg_pin.download(), vg.download()
+        assert all(np.array_equal(a[k], b[k]) for k in ("vstart", "vowner", "vcol", "vw", "outdeg"))
+        got, _ = vg_pin.run("sssp", "sync_push_dd", 0)
+        assert np.array_equal(got, oracle.dijkstra(n, s, d, w, 0))
+        x, _ = vg_pin.run("pr", "sync_push_td")
+        xr, _ = oracle.pagerank(n, s, d)
+        assert pr_l1(x, xr) <= PR_L1
