@@ -42,7 +42,7 @@ def _read_out(path, dtype):
 @pytest.fixture(scope="module")
 def graph(tmp_path_factory, gpu):
     s, d, w = gpu.gen_rmat(12, 8, seed=4, wmin=1, wmax=63)
-    n = 4096
+    n = int(max(s.max(), d.max())) + 1  # what the loader derives from the file (largest id + 1)
     p = tmp_path_factory.mktemp("g") / "g.wel"
     _write_wel(p, s, d, w)
     return p, n, s, d, w
