@@ -131,6 +131,20 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def reduce_job(total_ms: float, total_edges: float, world: int, device) -> tuple[float, float]:
+    """Whole-job time and work over the ranks: the slowest rank's time, the sum of all ranks' edges."""
+    if world <= 1:
+        return total_ms, total_edges
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([total_ms, total_edges], dtype=torch.float64, device=device)
+    mx, sm = t.clone(), t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(sm, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(sm[1])
+
+
 # ---------------------------------------------------------------- workload
 def make_inputs(E, scale: int):
     s, d, w = E.gen_rmat(scale, EF, seed=SEED, wmin=1, wmax=63)
@@ -214,15 +228,7 @@ def bench_gpu(args) -> None:
     total_ms = sum(step_ms)
     step_edges = sum(per_algo[a]["edges"][-1] for a, _ in ALGO_PLAN)
     total_edges = step_edges * args.steps
-    if world > 1:
-        t = torch.tensor([total_ms, total_edges], dtype=torch.float64, device=dev)
-        mx = t.clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sm_ = t.clone()
-        torch.distributed.all_reduce(sm_, op=torch.distributed.ReduceOp.SUM)
-        total_ms_all, total_edges_all = float(mx[0]), float(sm_[1])
-    else:
-        total_ms_all, total_edges_all = total_ms, total_edges
+    total_ms_all, total_edges_all = reduce_job(total_ms, total_edges, world, dev)
     value = total_edges_all / (total_ms_all * 1e-3) / 1e9
 
     # ---- end to end through the C ABI with host buffers (timed on the host around the whole step)
@@ -306,6 +312,56 @@ def bench_gpu(args) -> None:
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+GRID_SIDE, GRID_SEED = 4096, 7
+
+
+def bench_grid(args) -> None:
+    """High-diameter road-like graph: 4096 x 4096 grid, 4-neighbour undirected, 10 % of edges deleted,
+    0.1 % long-range shortcuts, weights U[1,1000], seed 7. BFS/SSSP/SSWP sync_push_dd from vertex 0, one
+    persistent launch each, against the same kernels run one launch per round with a host round trip
+    in between (the reference's loop shape, src/eegraph.cu:89-211)."""
+    import torch
+
+    import eegraph_gb300 as E
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    E.lib().eeg_set_device(local)
+    side = args.grid_side
+    n = side * side
+    s, d, w = E.gen_grid(side, 0.1, 0.001, seed=GRID_SEED, wmin=1, wmax=1000)
+    stream = torch.cuda.current_stream().cuda_stream
+    plan = [("bfs", "sync_push_dd"), ("sssp", "sync_push_dd"), ("sswp", "sync_push_dd")]
+    peak, peak_kind = load_peaks()
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    per = {}
+    with E.VirtualGraph.build(n, s, d, w, K=args.k, stream=stream) as vg, ClockSampler(local) as clk:
+        for algo, variant in plan:
+            for _ in range(args.warmup):
+                vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream)
+            pers = [vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream)[1] for _ in range(args.steps)]
+            hl = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, host_loop=True)[1]
+            ms = statistics.median(r["kernel_ms"] for r in pers)
+            r0 = pers[0]
+            per[algo] = {"kernel_ms": round(ms, 3), "rounds": r0["iterations"],
+                         "gteps": round(r0["reached_edges"] / (ms * 1e-3) / 1e9, 3),
+                         "roofline_frac": round(r0["algorithmic_bytes"] / (ms * 1e-3) / 1e9 / peak, 4),
+                         "host_loop_ms": round(hl["kernel_ms"], 3),
+                         "speedup_vs_host_loop": round(hl["kernel_ms"] / ms, 2)}
+    tot_ms = sum(v["kernel_ms"] for v in per.values())
+    tot_e = sum(float(r) for r in [per[a]["gteps"] * per[a]["kernel_ms"] * 1e6 for a in per])
+    line = {"metric": "GTEPS (BFS+SSSP+SSWP reached edges / device time) on the 4096^2 road-like grid",
+            "value": round(tot_e / (tot_ms * 1e-3) / 1e9, 3), "unit": "GTEPS", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(tot_ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grid, generated in-process)",
+            "config": {"workload": f"grid {side}x{side}, 10% edges deleted, 0.1% shortcuts, w~U[1,1000], seed 7, "
+                                   f"source 0, K={args.k}", "vertices": n, "arcs": int(s.size)},
+            "per_algo": per, "peak": peak, "peak_source": peak_kind, "clocks": clk.summary()}
+    print(json.dumps(line))
 
 
 # ---------------------------------------------------------------- CPU (reference) path
@@ -422,6 +478,9 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
     ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
                     help="subset of the step to run (profiling); the headline uses all five")
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "grid"],
+                    help="rmat: the headline (R-MAT s22, five algorithms); grid: the 4096^2 high-diameter graph")
+    ap.add_argument("--grid-side", type=int, default=GRID_SIDE)
     args = ap.parse_args()
     global ALGO_PLAN
     ALGO_PLAN = [p for p in ALGO_PLAN if p[0] in args.algos.split(",")]
@@ -429,6 +488,8 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         bench_reference(args)
+    elif args.workload == "grid":
+        bench_grid(args)
     else:
         bench_gpu(args)
 

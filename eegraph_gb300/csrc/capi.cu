@@ -394,7 +394,6 @@ EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, u
             r.reached_edges = mr;
             r.algorithmic_bytes = 12.0 * (double)nr + (op == OP_BFS ? 8.0 : 12.0) * (double)mr;
             r.gteps = r.kernel_ms > 0 ? (double)mr / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
-            r.launches = 2;  // persistent traversal kernel + reached-set statistics
         }
     }
     if (res) *res = r;

@@ -35,7 +35,7 @@ struct TravCtrl {
     uint32_t qparts[3];   // parts enqueued per round (rotating; TD: improvement flag)
     uint32_t qverts[3];   // vertices enqueued per round (rotating)
     uint32_t iterations;
-    uint32_t pad;
+    uint32_t done;        // the traversal reached its end (fixed point, cap or abort)
     unsigned long long parts_processed;
     unsigned long long edges_scanned;
     unsigned long long updates;

@@ -51,8 +51,10 @@ struct TravArgs {
     uint32_t seed_all;
     uint32_t partner;
     uint32_t max_iters;
-    uint32_t pad;
+    uint32_t it_start;     // first round of this launch (0: also the set-up phase)
     uint64_t timeout_ns;
+    uint32_t rounds_limit; // rounds this launch may run (host-loop mode: 1); 0 = until done
+    uint32_t pad2;
 };
 
 template <int OP>
@@ -149,24 +151,31 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     const uint64_t pol = l2_evict_first_policy();
     uint32_t epoch = 0;
 
-    // ---- round 0 set-up: values, stamps, initial frontier
-    for (uint32_t v = gtid; v < a.n; v += gthreads) {
-        a.dist[v] = init_value<OP>(v, a.source);
-        if (!TD) a.stamp[v] = 0u;
-    }
-    if (!TD && !a.seed_all && blockIdx.x == 0) {
-        const uint32_t s0 = a.vstart[a.source], s1 = a.vstart[a.source + 1];
-        for (uint32_t j = threadIdx.x; j < s1 - s0; j += T_TPB) a.q0[j] = s0 + j;
-        if (threadIdx.x == 0) {
-            ctrl->qparts[0] = s1 - s0;
-            ctrl->qverts[0] = 1u;
-        }
-    }
     unsigned long long my_parts = 0, my_edges = 0, my_updates = 0;
-    uint32_t it = 0;
-    if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
+    uint32_t it = a.it_start;
+    bool all_done = true;  // false when this launch stops only because of rounds_limit
+    if (a.it_start == 0) {
+        // ---- round 0 set-up: values, stamps, initial frontier
+        for (uint32_t v = gtid; v < a.n; v += gthreads) {
+            a.dist[v] = init_value<OP>(v, a.source);
+            if (!TD) a.stamp[v] = 0u;
+        }
+        if (!TD && !a.seed_all && blockIdx.x == 0) {
+            const uint32_t s0 = a.vstart[a.source], s1 = a.vstart[a.source + 1];
+            for (uint32_t j = threadIdx.x; j < s1 - s0; j += T_TPB) a.q0[j] = s0 + j;
+            if (threadIdx.x == 0) {
+                ctrl->qparts[0] = s1 - s0;
+                ctrl->qverts[0] = 1u;
+            }
+        }
+        if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
+    }
 
     for (;; ++it) {
+        if (a.rounds_limit && it - a.it_start >= a.rounds_limit) {  // host-loop mode: next round, next launch
+            all_done = false;
+            break;
+        }
         const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
         const bool dense = TD || (a.seed_all && it == 0);
         if (it > 0) {
@@ -274,7 +283,10 @@ finish:
         if (my_edges) atomicAdd(&ctrl->edges_scanned, my_edges);
         if (my_updates) atomicAdd(&ctrl->updates, my_updates);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->iterations = it;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctrl->iterations = it;
+        ctrl->done = all_done ? 1u : 0u;
+    }
 }
 
 // Reached-set statistics: n_r and m_r (out-edges of reached vertices).

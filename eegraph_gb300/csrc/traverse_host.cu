@@ -87,22 +87,37 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     a.partner = (variant == EEG_SYNC_PUSH_TD) ? 1u : 0u;
     a.max_iters = o.max_iterations ? o.max_iterations : (vg->n > 0xFFFFFFF0u ? 0xFFFFFFFFu : vg->n + 2u);
     a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
+    a.it_start = 0;
+    a.rounds_limit = o.host_loop ? 1u : 0u;
 
     EEG_CUDA(cudaEventRecord(ws.ev[0], st));
-    eeg_status s;
-    switch (op) {
-        case OP_BFS: s = launch_bfs(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
-        case OP_SSSP: s = launch_sssp(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
-        case OP_SSWP: s = launch_sswp(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
-        case OP_CC: s = launch_cc(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
-        default: set_last_error("unknown algorithm"); return EEG_ERR_INVALID;
+    TravCtrl hc;
+    uint32_t launches = 0;
+    for (;;) {
+        eeg_status s;
+        switch (op) {
+            case OP_BFS: s = launch_bfs(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
+            case OP_SSSP: s = launch_sssp(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
+            case OP_SSWP: s = launch_sswp(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
+            case OP_CC: s = launch_cc(a, td, vg->K, vg->device, o.blocks_per_sm, st); break;
+            default: set_last_error("unknown algorithm"); return EEG_ERR_INVALID;
+        }
+        if (s != EEG_OK) return s;
+        ++launches;
+        if (!o.host_loop) break;
+        // host-loop mode: read the round's outcome back before deciding on the next launch
+        EEG_CUDA(cudaMemcpyAsync(&hc, ws.tctrl, sizeof(TravCtrl), cudaMemcpyDeviceToHost, st));
+        EEG_CUDA(cudaStreamSynchronize(st));
+        if (hc.done || hc.bw.status != DEV_OK) break;
+        a.it_start = hc.iterations;
+        // every launch counts its barrier arrivals from zero
+        EEG_CUDA(cudaMemsetAsync(&ws.tctrl->bw.arrive, 0, sizeof(uint32_t), st));
     }
-    if (s != EEG_OK) return s;
     EEG_CUDA(cudaEventRecord(ws.ev[1], st));
 
-    TravCtrl hc;
     EEG_CUDA(cudaMemcpyAsync(&hc, ws.tctrl, sizeof(TravCtrl), cudaMemcpyDeviceToHost, st));
     EEG_CUDA(cudaStreamSynchronize(st));
+    if (res) res->launches = launches + 1;  // + the reached-set statistics kernel
     float ms = 0.f;
     EEG_CUDA(cudaEventElapsedTime(&ms, ws.ev[0], ws.ev[1]));
     if (res) {

@@ -195,7 +195,10 @@ typedef struct eeg_options {
     uint32_t blocks_per_sm;   /* 0 = as many as occupancy allows */
     uint32_t record_activity; /* 1: store active-vertex counts per iteration (reference --activity) */
     uint32_t timeout_ms;      /* bound on any device-side wait (0 = 10000 ms) */
-    uint32_t reserved[8];
+    uint32_t host_loop;       /* traversals: 1 = one launch per round with a host round trip in between,
+                                 as the reference's do { H2D flag; launch; sync; D2H flag } while loop
+                                 (src/eegraph.cu:89-211) -- for comparison; 0 = one persistent launch */
+    uint32_t reserved[7];
 } eeg_options;
 
 typedef struct eeg_result {

@@ -244,3 +244,22 @@ def test_build_from_page_locked_host_arrays(gpu):
         x, _ = vg_pin.run("pr", "sync_push_td")
         xr, _ = oracle.pagerank(n, s, d)
         assert pr_l1(x, xr) <= PR_L1
+
+
+@pytest.mark.parametrize("algo,variant", [("bfs", "sync_push_dd"), ("sssp", "async_push_dd"), ("cc", "sync_push_td"),
+                                          ("sswp", "async_push_td")])
+def test_host_loop_mode_equals_persistent(gpu, algo, variant):
+    """One launch per round with a host round trip (the reference's loop shape) gives the same values
+    and the same number of rounds as the single persistent launch."""
+    side = 48
+    n = side * side
+    s, d, w = gpu.gen_grid(side, 0.1, 0.01, seed=7, wmin=1, wmax=1000)
+    with gpu.VirtualGraph.build(n, s, d, w, K=4) as vg:
+        a, ra = vg.run(algo, variant, 0)
+        b, rb = vg.run(algo, variant, 0, host_loop=True)
+    assert np.array_equal(a, b)
+    assert np.array_equal(a, oracle.expected(algo, variant, n, s, d, w, 0))
+    if algo == "bfs":  # level-synchronous: the round count is the source's eccentricity + 1 either way
+        assert ra["iterations"] == rb["iterations"]
+    assert rb["launches"] == rb["iterations"] + 2  # one per round, the final check, the statistics kernel
+    assert ra["launches"] == 2

@@ -1,0 +1,51 @@
+"""Multi-rank host logic of the benchmark, on CPU with the gloo backend (world size 2).
+
+A single traversal does not shard (every round exchanges the frontier), so N GPUs run N independent
+replicas; the whole-job figure is the sum of the replicas' work over the slowest replica's time.
+"""
+import os
+import socket
+
+import pytest
+import torch.multiprocessing as mp
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    ms, edges = bench.reduce_job(10.0 + rank, 1000.0 * (rank + 1), world, "cpu")
+    q.put((rank, ms, edges))
+    dist.destroy_process_group()
+
+
+def test_reduce_job_two_ranks():
+    world, port = 2, _free_port()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    got = sorted(q.get(timeout=10) for _ in range(world))
+    for _, ms, edges in got:
+        assert ms == 11.0 and edges == 3000.0
+
+
+def test_reduce_job_single_rank_is_identity():
+    import bench
+
+    assert bench.reduce_job(5.0, 7.0, 1, "cpu") == (5.0, 7.0)
