@@ -39,6 +39,8 @@ EXPORTED = [
     "eeg_vgraph_build", "eeg_vgraph_build_arrays", "eeg_vgraph_get_info", "eeg_vgraph_download",
     "eeg_vgraph_export_reference_layout", "eeg_vgraph_destroy", "eeg_options_init", "eeg_run",
     "eeg_run_noalloc", "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
+    "eeg_batch_create", "eeg_batch_set_queries", "eeg_batch_query_offset", "eeg_batch_run", "eeg_batch_rounds",
+    "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k",
 ]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -116,6 +118,15 @@ def _load() -> C.CDLL:
                               vp, C.POINTER(Result)]),
         "eeg_run_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_uint32, C.c_uint64, C.c_uint32, vp, vp, vp, vp,
                                       C.c_uint32, vp, vp, C.POINTER(C.c_uint32)]),
+        "eeg_batch_create": (C.c_int, [C.POINTER(vp), C.c_uint32, C.POINTER(vp)]),
+        "eeg_batch_set_queries": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.POINTER(C.c_ulonglong)]),
+        "eeg_batch_query_offset": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_ulonglong)]),
+        "eeg_batch_run": (C.c_int, [vp, vp, vp, C.POINTER(C.c_float)]),
+        "eeg_batch_rounds": (C.c_int, [vp, vp]),
+        "eeg_batch_autotune": (C.c_int, [vp, vp, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
+        "eeg_batch_destroy": (None, [vp]),
+        "eeg_autotune_k": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32),
+                                     C.POINTER(C.c_float)]),
         "eeg_energy_begin": (C.c_int, [C.c_int, C.c_char_p, C.c_uint32, C.POINTER(vp)]),
         "eeg_energy_mark": (C.c_int, [vp]),
         "eeg_energy_end": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -350,6 +361,84 @@ class VirtualGraph:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- batched queries
+class Query(C.Structure):
+    _fields_ = [("graph", C.c_uint32), ("algo", C.c_uint32), ("source", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class Batch:
+    """Many BFS/SSSP/SSWP queries over many device graphs in one launch (eeg_batch_*)."""
+
+    def __init__(self, graphs):
+        self.graphs = list(graphs)  # keep them alive
+        arr = (C.c_void_p * len(self.graphs))(*[g._h.value for g in self.graphs])
+        h = C.c_void_p()
+        _check(_lib.eeg_batch_create(arr, len(self.graphs), C.byref(h)), "batch_create")
+        self._h = h
+        self.nq = 0
+
+    def set_queries(self, queries, cluster_size: int = 0) -> int:
+        """queries: iterable of (graph_index, algo, source); returns the output size in uint32 words."""
+        qs = [(g, ALGOS[a] if isinstance(a, str) else int(a), s) for g, a, s in queries]
+        arr = (Query * max(len(qs), 1))(*[Query(g, a, s, 0) for g, a, s in qs])
+        words = C.c_ulonglong()
+        _check(_lib.eeg_batch_set_queries(self._h, arr, len(qs), cluster_size, C.byref(words)), "batch_set_queries")
+        self.nq = len(qs)
+        self.out_words = words.value
+        return words.value
+
+    def offsets(self):
+        out = []
+        for i in range(self.nq):
+            o = C.c_ulonglong()
+            _check(_lib.eeg_batch_query_offset(self._h, i, C.byref(o)), "batch_query_offset")
+            out.append(o.value)
+        return out
+
+    def run(self, out_device_ptr: int, stream: int | None = None) -> float:
+        ms = C.c_float()
+        _check(_lib.eeg_batch_run(self._h, C.c_void_p(out_device_ptr), C.c_void_p(stream) if stream else None,
+                                  C.byref(ms)), "batch_run")
+        return ms.value
+
+    def rounds(self) -> np.ndarray:
+        r = np.zeros(max(self.nq, 1), np.uint32)
+        _check(_lib.eeg_batch_rounds(self._h, _ptr(r)), "batch_rounds")
+        return r[: self.nq]
+
+    def autotune(self, out_device_ptr: int):
+        c, ms = C.c_uint32(), C.c_float()
+        _check(_lib.eeg_batch_autotune(self._h, C.c_void_p(out_device_ptr), C.byref(c), C.byref(ms)), "batch_autotune")
+        return c.value, ms.value
+
+    def close(self):
+        if self._h:
+            _lib.eeg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def autotune_k(num_nodes: int, src, dst, w=None, reps: int = 3):
+    """Fastest part size K for this graph (BFS + SSSP from the max-degree vertex); (K, ms per K)."""
+    src, dst = _u32(src), _u32(dst)
+    wi = _u32(w) if w is not None else None
+    k = C.c_uint32()
+    ms = (C.c_float * 3)()
+    _check(_lib.eeg_autotune_k(num_nodes, src.size, _ptr(src), _ptr(dst), _ptr(wi), reps, C.byref(k), ms), "autotune_k")
+    return k.value, {4: ms[0], 8: ms[1], 16: ms[2]}
 
 
 # ---------------------------------------------------------------- energy

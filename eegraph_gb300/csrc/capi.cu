@@ -4,9 +4,13 @@
 // src/eegraph.cu) at the C level: handles own their device memory, results go to caller-owned
 // buffers, every failure is a returned status (the reference calls exit(), include/gpu_error_check.cuh:8-16).
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "internal.hpp"
@@ -324,6 +328,54 @@ EEG_API eeg_status eeg_vgraph_export_reference_layout(const eeg_vgraph* vg, uint
             }
         }
     }
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_autotune_k(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                  const uint32_t* weight, uint32_t reps, uint32_t* best_k, float* ms_per_k) {
+    if (!best_k) {
+        set_last_error("eeg_autotune_k: null output");
+        return EEG_ERR_INVALID;
+    }
+    static std::mutex mu;
+    static std::map<std::tuple<uint32_t, uint64_t, uint32_t>, std::pair<uint32_t, std::array<float, 3>>> cache;
+    reps = reps ? reps : 3;
+    const uint32_t ks[3] = {4, 8, 16};
+    std::array<float, 3> times{};
+    std::tuple<uint32_t, uint64_t, uint32_t> key;
+    for (int i = 0; i < 3; ++i) {
+        eeg_vgraph* vg = nullptr;
+        EEG_TRY(eeg_vgraph_build_arrays(num_nodes, num_edges, src, dst, weight, ks[i], 0, nullptr, &vg));
+        if (i == 0) {
+            key = std::make_tuple(num_nodes, num_edges, vg->max_deg);
+            std::lock_guard<std::mutex> lk(mu);
+            auto it = cache.find(key);
+            if (it != cache.end()) {
+                eeg_vgraph_destroy(vg);
+                *best_k = it->second.first;
+                if (ms_per_k) std::copy(it->second.second.begin(), it->second.second.end(), ms_per_k);
+                return EEG_OK;
+            }
+        }
+        std::vector<float> t;
+        eeg_status s = EEG_OK;
+        for (uint32_t r = 0; r < reps + 1 && s == EEG_OK; ++r) {  // first run warms up
+            eeg_result a{}, b{};
+            s = eeg_run(vg, EEG_BFS, EEG_SYNC_PUSH_DD, vg->max_deg_vertex, nullptr, nullptr, 0, nullptr, 0, nullptr, &a);
+            if (s == EEG_OK)
+                s = eeg_run(vg, EEG_SSSP, EEG_SYNC_PUSH_DD, vg->max_deg_vertex, nullptr, nullptr, 0, nullptr, 0, nullptr, &b);
+            if (r > 0) t.push_back(a.kernel_ms + b.kernel_ms);
+        }
+        eeg_vgraph_destroy(vg);
+        if (s != EEG_OK) return s;
+        std::sort(t.begin(), t.end());
+        times[i] = t[t.size() / 2];
+    }
+    const int best = (int)(std::min_element(times.begin(), times.end()) - times.begin());
+    *best_k = ks[best];
+    if (ms_per_k) std::copy(times.begin(), times.end(), ms_per_k);
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = std::make_pair(ks[best], times);
     return EEG_OK;
 }
 

@@ -90,13 +90,14 @@ constexpr int WCAP = 256;  // per-warp append buffer (claimed vertices) before a
 // Warp-cooperative append of the warp's claimed vertices to the next queue: one reservation per flush
 // (atomicAdd of the parts total), then every claimed vertex's part ids are written; a vertex with more
 // than 32 parts is written by the whole warp. Called by all 32 lanes with a warp-uniform `cnt`.
-__device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
-                                           uint32_t nxt, uint32_t lane) {
+__device__ __forceinline__ void warp_append(const uint32_t* __restrict__ vstart, uint32_t* parts_ctr,
+                                            uint32_t* verts_ctr, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
+                                            uint32_t lane) {
     __syncwarp();
     uint32_t sum = 0;
     for (uint32_t e = lane; e < cnt; e += 32u) {
         const uint32_t t = buf[e];
-        sum += a.vstart[t + 1] - a.vstart[t];
+        sum += vstart[t + 1] - vstart[t];
     }
     uint32_t inc = sum;
 #pragma unroll
@@ -107,8 +108,8 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
     const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
     uint32_t base = 0;
     if (lane == 0) {
-        if (total) base = atomicAdd(&a.ctrl->qparts[nxt], total);
-        atomicAdd(&a.ctrl->qverts[nxt], cnt);
+        if (total) base = atomicAdd(parts_ctr, total);
+        if (verts_ctr) atomicAdd(verts_ctr, cnt);
     }
     base = __shfl_sync(0xffffffffu, base, 0);
     uint32_t pos = base + inc - sum;
@@ -118,8 +119,8 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
         uint32_t s0 = 0, np = 0;
         if (e < cnt) {
             const uint32_t t = buf[e];
-            s0 = a.vstart[t];
-            np = a.vstart[t + 1] - s0;
+            s0 = vstart[t];
+            np = vstart[t + 1] - s0;
             if (np <= 32u)
                 for (uint32_t j = 0; j < np; ++j) qnext[pos + j] = s0 + j;
         }
@@ -135,6 +136,11 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
         pos += np;
     }
     __syncwarp();
+}
+
+__device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
+                                           uint32_t nxt, uint32_t lane) {
+    warp_append(a.vstart, &a.ctrl->qparts[nxt], &a.ctrl->qverts[nxt], buf, cnt, qnext, lane);
 }
 
 template <int OP, int K, bool TD>

@@ -235,6 +235,42 @@ EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, u
                            const eeg_options* opts, void* out, int out_on_device, uint32_t* activity,
                            uint32_t activity_cap, void* stream, eeg_result* res);
 
+/* ------------------------------------------------------------------ batched queries */
+
+/* Many BFS/SSSP/SSWP queries over many device virtual graphs in ONE launch. No counterpart in the
+ * reference, which runs each query as a separate eegraph_<algo> call (src/main.cu:74-281).
+ * A persistent kernel made of thread-block clusters takes queries from a device work queue (largest
+ * graphs first) and runs each traversal on one cluster (rounds separated by the hardware cluster
+ * barrier); the launch is captured once in a CUDA graph and replayed by eeg_batch_run. Results equal
+ * eeg_run's for the same (graph, algorithm, source). Graphs must stay alive while the batch is used. */
+typedef struct eeg_batch eeg_batch;
+typedef struct eeg_query {
+    uint32_t graph;    /* index into the graphs given to eeg_batch_create */
+    uint32_t algo;     /* EEG_BFS, EEG_SSSP or EEG_SSWP */
+    uint32_t source;
+    uint32_t reserved;
+} eeg_query;
+EEG_API eeg_status eeg_batch_create(eeg_vgraph* const* graphs, uint32_t num_graphs, eeg_batch** out);
+/* Set the queries; *out_words receives the output size: query i writes num_nodes(graph_i) uint32 values
+ * at eeg_batch_query_offset(i) (queries laid out in the given order). cluster_size: CTAs per query
+ * (1, 2, 4 or 8; 0 = 4). */
+EEG_API eeg_status eeg_batch_set_queries(eeg_batch* b, const eeg_query* queries, uint32_t num_queries,
+                                         uint32_t cluster_size, unsigned long long* out_words);
+EEG_API eeg_status eeg_batch_query_offset(const eeg_batch* b, uint32_t query, unsigned long long* offset);
+/* Run every query (device output arena `out`); ordered after `stream`; *ms = device time of the launch. */
+EEG_API eeg_status eeg_batch_run(eeg_batch* b, uint32_t* out, void* stream, float* ms);
+/* Rounds each query took (num_queries entries, query order). */
+EEG_API eeg_status eeg_batch_rounds(const eeg_batch* b, uint32_t* rounds);
+/* Autotuner: time the batch with 1, 2, 4 and 8 CTAs per query and keep the fastest. */
+EEG_API eeg_status eeg_batch_autotune(eeg_batch* b, uint32_t* out, uint32_t* chosen_cluster_size, float* best_ms);
+EEG_API void eeg_batch_destroy(eeg_batch* b);
+
+/* Autotuner for the part size: builds the graph with K = 4, 8 and 16, times BFS and SSSP from the
+ * highest-out-degree vertex (median of `reps`), and returns the fastest K; ms_per_k (may be NULL)
+ * receives the three times. Results are cached per (num_nodes, num_edges, max out-degree). Host arrays. */
+EEG_API eeg_status eeg_autotune_k(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                  const uint32_t* weight, uint32_t reps, uint32_t* best_k, float* ms_per_k);
+
 /* Allocation-free traversal run. No counterpart in the reference: it exists for callers that cannot
  * allocate device memory when they run a query -- plugins whose host application owns all GPU memory,
  * frameworks that route every allocation through their own pool, service loops where cudaMalloc's

