@@ -40,7 +40,7 @@ EXPORTED = [
     "eeg_vgraph_export_reference_layout", "eeg_vgraph_destroy", "eeg_options_init", "eeg_run",
     "eeg_run_noalloc", "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
     "eeg_batch_create", "eeg_batch_set_queries", "eeg_batch_query_offset", "eeg_batch_run", "eeg_batch_rounds",
-    "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k",
+    "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_batch_query_times",
 ]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -123,6 +123,7 @@ def _load() -> C.CDLL:
         "eeg_batch_query_offset": (C.c_int, [vp, C.c_uint32, C.POINTER(C.c_ulonglong)]),
         "eeg_batch_run": (C.c_int, [vp, vp, vp, C.POINTER(C.c_float)]),
         "eeg_batch_rounds": (C.c_int, [vp, vp]),
+        "eeg_batch_query_times": (C.c_int, [vp, vp]),
         "eeg_batch_autotune": (C.c_int, [vp, vp, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
         "eeg_batch_destroy": (None, [vp]),
         "eeg_autotune_k": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32),
@@ -407,6 +408,12 @@ class Batch:
         r = np.zeros(max(self.nq, 1), np.uint32)
         _check(_lib.eeg_batch_rounds(self._h, _ptr(r)), "batch_rounds")
         return r[: self.nq]
+
+    def query_times(self) -> np.ndarray:
+        """(num_queries, 3): start ns, end ns, cluster index of each query in the last run."""
+        t = np.zeros(3 * max(self.nq, 1), np.uint64)
+        _check(_lib.eeg_batch_query_times(self._h, _ptr(t)), "batch_query_times")
+        return t[: 3 * self.nq].reshape(-1, 3)
 
     def autotune(self, out_device_ptr: int):
         c, ms = C.c_uint32(), C.c_float()

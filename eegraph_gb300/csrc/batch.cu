@@ -49,6 +49,7 @@ struct BArgs {
     uint32_t* next;     // work counter
     uint32_t* out;      // output arena
     uint32_t* rounds;   // per query (input order)
+    unsigned long long* times;  // per query (input order): start and end (%globaltimer ns) and cluster id
     uint32_t* q0;       // per cluster: 2 * qcap part ids
     uint32_t* stamp;    // per cluster: scap stamps
     BCtrl* ctrl;        // per cluster
@@ -165,13 +166,19 @@ __global__ void __launch_bounds__(B_TPB, 2) k_batch(BArgs a) {
         if (qi >= a.nq) break;
         const BQuery q = a.queries[qi];
         const BGraph g = a.graphs[q.graph];
+        const unsigned long long t0 = global_timer_ns();
         uint32_t rounds;
         switch (q.op) {
             case OP_BFS: rounds = dispatch_k<OP_BFS>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
             case OP_SSSP: rounds = dispatch_k<OP_SSSP>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
             default: rounds = dispatch_k<OP_SSWP>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
         }
-        if (crank == 0 && threadIdx.x == 0) a.rounds[q.input_index] = rounds;
+        if (crank == 0 && threadIdx.x == 0) {
+            a.rounds[q.input_index] = rounds;
+            a.times[3 * (size_t)q.input_index] = t0;
+            a.times[3 * (size_t)q.input_index + 1] = global_timer_ns();
+            a.times[3 * (size_t)q.input_index + 2] = cid;
+        }
     }
     if (crank == 0 && threadIdx.x == 0) ctrl->tag = tag;
 }
@@ -192,6 +199,7 @@ struct eeg_batch {
     unsigned long long out_words = 0;
     uint32_t* d_next = nullptr;
     uint32_t* d_rounds = nullptr;
+    unsigned long long* d_times = nullptr;
     uint32_t* d_q = nullptr;
     uint32_t* d_stamp = nullptr;
     BCtrl* d_ctrl = nullptr;
@@ -226,6 +234,7 @@ eeg_status launch(eeg_batch* b, uint32_t* out) {
     a.next = b->d_next;
     a.out = out;
     a.rounds = b->d_rounds;
+    a.times = b->d_times;
     a.q0 = b->d_q;
     a.stamp = b->d_stamp;
     a.ctrl = b->d_ctrl;
@@ -371,10 +380,13 @@ EEG_API eeg_status eeg_batch_set_queries(eeg_batch* b, const eeg_query* queries,
     });
     cudaFree(b->d_queries);
     cudaFree(b->d_rounds);
+    cudaFree(b->d_times);
     b->d_queries = nullptr;
     b->d_rounds = nullptr;
+    b->d_times = nullptr;
     EEG_CUDA(cudaMalloc((void**)&b->d_queries, sizeof(BQuery) * std::max<uint32_t>(nq, 1)));
     EEG_CUDA(cudaMalloc((void**)&b->d_rounds, sizeof(uint32_t) * std::max<uint32_t>(nq, 1)));
+    EEG_CUDA(cudaMalloc((void**)&b->d_times, 3 * sizeof(unsigned long long) * std::max<uint32_t>(nq, 1)));
     if (nq) EEG_CUDA(cudaMemcpy(b->d_queries, hq.data(), sizeof(BQuery) * nq, cudaMemcpyHostToDevice));
     b->nq = nq;
     b->out_words = off;
@@ -422,6 +434,15 @@ EEG_API eeg_status eeg_batch_rounds(const eeg_batch* b, uint32_t* rounds) {
     return EEG_OK;
 }
 
+EEG_API eeg_status eeg_batch_query_times(const eeg_batch* b, unsigned long long* times) {
+    if (!b || !times) {
+        set_last_error("eeg_batch_query_times: null argument");
+        return EEG_ERR_INVALID;
+    }
+    if (b->nq) EEG_CUDA(cudaMemcpy(times, b->d_times, 3 * sizeof(unsigned long long) * b->nq, cudaMemcpyDeviceToHost));
+    return EEG_OK;
+}
+
 EEG_API eeg_status eeg_batch_autotune(eeg_batch* b, uint32_t* out, uint32_t* chosen_cluster_size, float* best_ms) {
     if (!b || (b->nq && !out)) {
         set_last_error("eeg_batch_autotune: null argument");
@@ -456,6 +477,7 @@ EEG_API void eeg_batch_destroy(eeg_batch* b) {
     cudaFree(b->d_queries);
     cudaFree(b->d_next);
     cudaFree(b->d_rounds);
+    cudaFree(b->d_times);
     if (b->ev[0]) cudaEventDestroy(b->ev[0]);
     if (b->ev[1]) cudaEventDestroy(b->ev[1]);
     if (b->st) cudaStreamDestroy(b->st);

@@ -261,6 +261,9 @@ EEG_API eeg_status eeg_batch_query_offset(const eeg_batch* b, uint32_t query, un
 EEG_API eeg_status eeg_batch_run(eeg_batch* b, uint32_t* out, void* stream, float* ms);
 /* Rounds each query took (num_queries entries, query order). */
 EEG_API eeg_status eeg_batch_rounds(const eeg_batch* b, uint32_t* rounds);
+/* Per query (query order) of the last run: device start and end time (ns, global timer) and the
+ * index of the cluster that ran it -- 3 values per query. */
+EEG_API eeg_status eeg_batch_query_times(const eeg_batch* b, unsigned long long* times);
 /* Autotuner: time the batch with 1, 2, 4 and 8 CTAs per query and keep the fastest. */
 EEG_API eeg_status eeg_batch_autotune(eeg_batch* b, uint32_t* out, uint32_t* chosen_cluster_size, float* best_ms);
 EEG_API void eeg_batch_destroy(eeg_batch* b);
