@@ -392,6 +392,166 @@ def bench_batch(args) -> None:
     print(json.dumps(line))
 
 
+PPR_SCALE, PPR_COLS, PPR_SEEDS = 20, 64, 32
+
+
+def make_ppr_inputs(E, scale: int, cols: int = PPR_COLS, seed: int = 1):
+    """R-MAT (scale, edge factor 16, a/b/c/d .57/.19/.19/.05, seed 1) with FP32 weights U(0,1]; `cols`
+    teleport vectors, each uniform over 32 random seed vertices; dLoss/dX = c ~ N(0,1) (loss sum c*x)."""
+    n = 1 << scale
+    s, d, _ = E.gen_rmat(scale, EF, seed=seed, wmin=1, wmax=63)
+    rng = np.random.default_rng(seed)
+    w = (1.0 - rng.random(s.size)).astype(np.float32)
+    T = np.zeros((n, cols), np.float32)
+    for k in range(cols):
+        T[rng.choice(n, PPR_SEEDS, replace=False), k] = 1.0 / PPR_SEEDS
+    G = rng.standard_normal((n, cols)).astype(np.float32)
+    return n, np.asarray(s, np.uint32), np.asarray(d, np.uint32), w, T, G
+
+
+def ppr_cpu_baseline(budget_s: float, scale: int = 14, cols: int = 64) -> dict:
+    """FP64 oracle (one core) on a bounded sample: R-MAT s14 with the same shape of inputs; its
+    throughput is scaled to the full workload by the work ratio (edges x sweeps)."""
+    import eegraph_gb300 as E
+
+    import oracle
+
+    n, s, d, w, T, G = make_ppr_inputs(E, scale, cols)
+    t0 = time.perf_counter()
+    r = oracle.ppr(n, s, d, w.astype(np.float64), T, G, tol=1e-7)
+    dt = time.perf_counter() - t0
+    return {"grads_per_s_sample": cols / dt, "sample_edges": int(s.size), "sample_sweeps": int(sum(r["sweeps"])),
+            "seconds": dt}
+
+
+def bench_ppr(args) -> None:
+    """Differentiable personalised PageRank: forward + adjoint + gradients for 64 teleport vectors in
+    one batched call pair, against the single-column kernels looped per teleport vector."""
+    import torch
+
+    import eegraph_gb300 as E
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    E.lib().eeg_set_device(local)
+    scale = args.scale if args.scale != SCALE else PPR_SCALE
+    n, s, d, w, T, G = make_ppr_inputs(E, scale)
+    C = T.shape[1]
+    m = int(s.size)
+    stream = torch.cuda.current_stream().cuda_stream
+    vg = E.VirtualGraph.build(n, s, d, None, K=args.k, reverse=True, edge_ids=True, stream=stream)
+    dev = torch.device("cuda", local)
+    Tt, Gt = torch.from_numpy(T).to(dev), torch.from_numpy(G).to(dev)
+    X = torch.empty_like(Tt)
+    dT = torch.empty_like(Tt)
+    dw = torch.empty(m, dtype=torch.float32, device=dev)
+    dwn = torch.empty(m, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    outs = {"dw": dw.data_ptr(), "dwn": dwn.data_ptr(), "dt": dT.data_ptr()}
+    with E.PPR(vg, C) as pb, ClockSampler(local) as clk:
+        pb.set_weights(w)
+        step_ms, fwd, adj = [], [], []
+        for i in range(args.warmup + args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            ev0.record()
+            _, rf = pb.forward(Tt.data_ptr(), X.data_ptr(), stream=stream)
+            _, ra = pb.adjoint(Gt.data_ptr(), out_ptrs=outs, stream=stream)
+            ev1.record()
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                step_ms.append(ev0.elapsed_time(ev1))
+                fwd.append(rf)
+                adj.append(ra)
+        Xb, dwb, dTb = X.cpu().numpy(), dw.cpu().numpy(), dT.cpu().numpy()
+        duality = abs(float((Gt.double() * X.double()).sum()) - float((Tt.double() * dT.double()).sum()))
+        duality /= float((Gt.double() * X.double()).abs().sum())
+        # end to end through the host API: pinned host inputs in, gradients out to host
+        Th, Gh = torch.from_numpy(T).pin_memory(), torch.from_numpy(G).pin_memory()
+        dw_h = torch.empty(m, dtype=torch.float32).pin_memory()
+        dT_h = torch.empty((n, C), dtype=torch.float32).pin_memory()
+        e2e_ms = []
+        for i in range(0 if args.no_e2e else args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pb.forward(Th.numpy(), False, stream=stream)
+            pb.adjoint(Gh.numpy(), out_host={"dw": dw_h.numpy(), "dt": dT_h.numpy()}, stream=stream)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                e2e_ms.append((time.perf_counter() - t0) * 1e3)
+        # plain: the single-column kernels looped over the teleport vectors (inputs pre-split per column)
+        Tc = Tt.t().contiguous()
+        Gc = Gt.t().contiguous()
+        Xc = torch.empty_like(Tc)
+        dTc = torch.empty_like(Tc)
+        dw1 = torch.empty(m, dtype=torch.float32, device=dev)
+        loop_ms = []
+        with E.PPR(vg, 1) as p1:
+            p1.set_weights(w)
+            for rep in range(2):
+                flush.zero_()
+                torch.cuda.synchronize()
+                ev0.record()
+                for k in range(C):
+                    p1.forward(Tc[k].data_ptr(), Xc[k].data_ptr(), stream=stream)
+                    last = {"dw": dw1.data_ptr(), "dt": dTc[k].data_ptr()} if k == C - 1 else {"dt": dTc[k].data_ptr()}
+                    p1.adjoint(Gc[k].data_ptr(), out_ptrs=last, accumulate=k > 0, stream=stream)
+                ev1.record()
+                torch.cuda.synchronize()
+                if rep > 0:
+                    loop_ms.append(ev0.elapsed_time(ev1))
+        def nl1(a, b):
+            return float((a - b).abs().sum() / b.abs().sum())
+        parity = {"X_nl1": nl1(Xc.t().double(), X.double()), "dT_nl1": nl1(dTc.t().double(), dT.double()),
+                  "dw_rel_l1": nl1(dw1.double(), dw.double()), "duality_rel": duality}
+    vg.close()
+    bms = statistics.median(step_ms)
+    lms = statistics.median(loop_ms)
+    fkm = statistics.median(r["kernel_ms"] for r in fwd)
+    fby = statistics.median(r["algorithmic_bytes"] for r in fwd)
+    fit = int(statistics.median(r["iterations"] for r in fwd))
+    ait = int(statistics.median(r["iterations"] for r in adj))
+    peak, peak_kind = load_peaks()
+    ach = fby / (fkm * 1e-3) / 1e9
+    h2d = 2 * n * C * 4
+    d2h = m * 4 + n * C * 4
+    line = {
+        "metric": "PR-grad/s (personalised PageRank forward + implicit adjoint + edge/teleport gradients, "
+                  "teleport vectors per second)",
+        "value": round(C / (bms * 1e-3), 2), "unit": "PR-grad/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(bms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP64 stop-test reduction)",
+        "data": "synthetic (seeded R-MAT, weights U(0,1], teleports and c generated in-process)",
+        "config": {"workload": f"R-MAT s{scale} ef{EF}, {C} teleport vectors x {PPR_SEEDS} seeds, d=0.85, "
+                               f"tol 1e-7, K={args.k}", "vertices": n, "edges": m, "columns": C,
+                   "l2": "iterates 2 x n x 64 x 4 B larger than L2; 256 MB L2 flush between timed steps"},
+        "sweeps": {"forward": fit, "adjoint": ait},
+        "plain_loop": {"ms_per_step": round(lms, 3), "grads_per_s": round(C / (lms * 1e-3), 2)},
+        "speedup_vs_plain_loop": round(lms / bms, 2),
+        "parity_batched_vs_loop": parity,
+        "roofline": {"bound": "hbm", "kernel": "k_ppr_rows (forward solve)", "achieved": round(ach, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_kind,
+                     "traffic": load_traffic("k_ppr_rows", f"ppr_s{scale}_k{args.k}")},
+        "e2e": {"value": round(C / (statistics.median(e2e_ms) * 1e-3), 2) if e2e_ms else None, "unit": "PR-grad/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": round(statistics.median(e2e_ms), 3) if e2e_ms else None},
+        "gpu_launches": 5,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        cb = ppr_cpu_baseline(args.cpu_budget)
+        work_full = m * (fit + ait)
+        work_sample = cb["sample_edges"] * cb["sample_sweeps"]
+        line["cpu_baseline"] = {"value": round(cb["grads_per_s_sample"] * work_sample / work_full, 4),
+                                "unit": "PR-grad/s", "cores": 1, "kind": "port",
+                                "sample": f"FP64 oracle, R-MAT s14 x 64 columns ({cb['seconds']:.1f} s), "
+                                          "scaled by edges x sweeps to the full workload"}
+    print(json.dumps(line))
+
+
 GRID_SIDE, GRID_SEED = 4096, 7
 
 
@@ -556,9 +716,10 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
     ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
                     help="subset of the step to run (profiling); the headline uses all five")
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "grid", "batch"],
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "grid", "batch", "ppr"],
                     help="rmat: the headline (R-MAT s22, five algorithms); grid: the 4096^2 high-diameter graph; "
-                         "batch: 256-graph query mixture, batched vs looped")
+                         "batch: 256-graph query mixture, batched vs looped; "
+                         "ppr: personalised PageRank forward + adjoint, 64 teleport vectors, batched vs looped")
     ap.add_argument("--batch-graphs", type=int, default=256)
     ap.add_argument("--grid-side", type=int, default=GRID_SIDE)
     args = ap.parse_args()
@@ -572,6 +733,8 @@ def main() -> None:
         bench_grid(args)
     elif args.workload == "batch":
         bench_batch(args)
+    elif args.workload == "ppr":
+        bench_ppr(args)
     else:
         bench_gpu(args)
 

@@ -28,7 +28,7 @@ VARIANTS = {"async_push_td": ASYNC_PUSH_TD, "async_push_dd": ASYNC_PUSH_DD,
             "sync_push_td": SYNC_PUSH_TD, "sync_push_dd": SYNC_PUSH_DD}
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 DIST_INFINITY = 4294967294
-VG_REVERSE, VG_MANAGED, VG_INPUT_DEVICE, VG_SHIFT_ONE = 1, 2, 4, 8
+VG_REVERSE, VG_MANAGED, VG_INPUT_DEVICE, VG_SHIFT_ONE, VG_EDGE_IDS = 1, 2, 4, 8, 16
 
 # every function the C header declares (checked by the CPU test suite)
 EXPORTED = [
@@ -41,6 +41,7 @@ EXPORTED = [
     "eeg_run_noalloc", "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
     "eeg_batch_create", "eeg_batch_set_queries", "eeg_batch_query_offset", "eeg_batch_run", "eeg_batch_rounds",
     "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_batch_query_times",
+    "eeg_ppr_create", "eeg_ppr_set_weights", "eeg_ppr_forward", "eeg_ppr_adjoint", "eeg_ppr_destroy",
 ]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -128,6 +129,12 @@ def _load() -> C.CDLL:
         "eeg_batch_destroy": (None, [vp]),
         "eeg_autotune_k": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32),
                                      C.POINTER(C.c_float)]),
+        "eeg_ppr_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
+        "eeg_ppr_set_weights": (C.c_int, [vp, vp, C.c_int]),
+        "eeg_ppr_forward": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, C.POINTER(Options), vp, C.POINTER(Result)]),
+        "eeg_ppr_adjoint": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.POINTER(Options), vp,
+                                      C.POINTER(Result)]),
+        "eeg_ppr_destroy": (None, [vp]),
         "eeg_energy_begin": (C.c_int, [C.c_int, C.c_char_p, C.c_uint32, C.POINTER(vp)]),
         "eeg_energy_mark": (C.c_int, [vp]),
         "eeg_energy_end": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -264,9 +271,10 @@ class VirtualGraph:
 
     @classmethod
     def build(cls, num_nodes: int, src, dst, w=None, K: int = 8, reverse: bool = False, managed: bool = False,
-              stream: int | None = None, shift_one: bool = False) -> "VirtualGraph":
+              stream: int | None = None, shift_one: bool = False, edge_ids: bool = False) -> "VirtualGraph":
         """Build from host arrays (copied to the device inside the call)."""
         flags = (VG_REVERSE if reverse else 0) | (VG_MANAGED if managed else 0) | (VG_SHIFT_ONE if shift_one else 0)
+        flags |= VG_EDGE_IDS if edge_ids else 0
         h = C.c_void_p()
         src, dst = _u32(src), _u32(dst)
         wi = _u32(w) if w is not None else None
@@ -276,8 +284,8 @@ class VirtualGraph:
 
     @classmethod
     def build_device(cls, num_nodes: int, num_edges: int, src_ptr: int, dst_ptr: int, w_ptr: int | None, K: int = 8,
-                     reverse: bool = False, stream: int | None = None) -> "VirtualGraph":
-        flags = VG_INPUT_DEVICE | (VG_REVERSE if reverse else 0)
+                     reverse: bool = False, stream: int | None = None, edge_ids: bool = False) -> "VirtualGraph":
+        flags = VG_INPUT_DEVICE | (VG_REVERSE if reverse else 0) | (VG_EDGE_IDS if edge_ids else 0)
         h = C.c_void_p()
         _check(_lib.eeg_vgraph_build_arrays(num_nodes, num_edges, C.c_void_p(src_ptr), C.c_void_p(dst_ptr),
                                             C.c_void_p(w_ptr) if w_ptr else None, K, flags,
@@ -423,6 +431,119 @@ class Batch:
     def close(self):
         if self._h:
             _lib.eeg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PPR:
+    """Differentiable personalised PageRank on a virtual graph built with reverse=True, edge_ids=True
+    (C ABI eeg_ppr_*). columns=1 runs the single-column kernels, 2..64 the batched row kernels.
+    Array arguments are numpy arrays (host) or device pointers given as ints."""
+
+    def __init__(self, vg: VirtualGraph, columns: int):
+        self._h = C.c_void_p()
+        self.vg = vg
+        self.columns = columns
+        inf = vg.info()
+        self.n, self.m = inf["num_nodes"], inf["num_edges"]
+        _check(_lib.eeg_ppr_create(vg._h, columns, C.byref(self._h)), "ppr_create")
+
+    @staticmethod
+    def _opts(tol, damping, max_iterations, timeout_ms):
+        o = Options()
+        _lib.eeg_options_init(C.byref(o))
+        o.pr_tolerance = tol
+        o.pr_damping = damping
+        o.max_iterations = max_iterations
+        o.timeout_ms = timeout_ms
+        return o
+
+    @staticmethod
+    def _arg(a, dtype=np.float32):
+        if a is None:
+            return None, 0, None
+        if isinstance(a, int):
+            return C.c_void_p(a), 1, None
+        arr = np.ascontiguousarray(a, dtype=dtype)
+        return C.c_void_p(arr.ctypes.data), 0, arr
+
+    def set_weights(self, w) -> None:
+        p, dev, keep = self._arg(w)
+        _check(_lib.eeg_ppr_set_weights(self._h, p, dev), "ppr_set_weights")
+
+    def forward(self, teleport, x_out=None, *, tol=0.0, damping=0.0, max_iterations=0, timeout_ms=0, stream=None,
+                check=True):
+        """teleport: n x columns (host array or device pointer). Returns (X or None, result dict).
+        x_out: device pointer (int) to write X to; with a host teleport and no x_out, X is returned."""
+        tp, tdev, keep = self._arg(teleport)
+        o = self._opts(tol, damping, max_iterations, timeout_ms)
+        r = Result()
+        if isinstance(x_out, int):
+            xp, xdev, xh = C.c_void_p(x_out), 1, None
+        elif x_out is False:
+            xp, xdev, xh = None, 0, None
+        else:
+            xh = np.empty((self.n, self.columns), np.float32)
+            xp, xdev = C.c_void_p(xh.ctypes.data), 0
+        st = _lib.eeg_ppr_forward(self._h, tp, tdev, xp, xdev, C.byref(o), C.c_void_p(stream) if stream else None,
+                                  C.byref(r))
+        if check:
+            _check(st, "ppr_forward")
+        res = r.as_dict()
+        res["status"] = st
+        return xh, res
+
+    def adjoint(self, dl_dx, *, outputs=("dw", "dwn", "dt"), out_ptrs=None, out_host=None, accumulate=False,
+                tol=0.0, damping=0.0, max_iterations=0, timeout_ms=0, stream=None, check=True):
+        """dl_dx: n x columns. Host mode returns dict of numpy arrays for the requested outputs
+        (dw: raw-weight gradient, dwn: normalised-weight gradient, dt: teleport gradient), written into
+        out_host's arrays when given; device mode writes to out_ptrs = {"dw": ptr, ...}."""
+        gp, gdev, keep = self._arg(dl_dx)
+        o = self._opts(tol, damping, max_iterations, timeout_ms)
+        r = Result()
+        out = {}
+        if out_ptrs is not None:
+            ptr = {k: C.c_void_p(v) for k, v in out_ptrs.items()}
+            on_dev = 1
+        elif out_host is not None:
+            out = dict(out_host)
+            for k, v in out.items():
+                if not (v.flags.c_contiguous and v.dtype == np.float32):
+                    raise ValueError(f"out_host[{k!r}] must be a C-contiguous float32 array")
+            ptr = {k: C.c_void_p(v.ctypes.data) for k, v in out.items()}
+            on_dev = 0
+        else:
+            if "dw" in outputs:
+                out["dw"] = np.empty(self.m, np.float32)
+            if "dwn" in outputs:
+                out["dwn"] = np.empty(self.m, np.float32)
+            if "dt" in outputs:
+                out["dt"] = np.empty((self.n, self.columns), np.float32)
+            ptr = {k: C.c_void_p(v.ctypes.data) for k, v in out.items()}
+            on_dev = 0
+        st = _lib.eeg_ppr_adjoint(self._h, gp, gdev, ptr.get("dt"), ptr.get("dw"), ptr.get("dwn"), on_dev,
+                                  1 if accumulate else 0, C.byref(o), C.c_void_p(stream) if stream else None,
+                                  C.byref(r))
+        if check:
+            _check(st, "ppr_adjoint")
+        res = r.as_dict()
+        res["status"] = st
+        return out, res
+
+    def close(self):
+        if self._h:
+            _lib.eeg_ppr_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):

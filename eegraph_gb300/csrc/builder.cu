@@ -149,10 +149,11 @@ constexpr int R_TILE = R_TPB * R_ITEMS;
 constexpr int R_BINS = 256;
 static_assert(R_TPB == R_BINS, "one thread per digit in the cross-warp prefix");
 
-// 0-based owner/neighbour (+ weight) into the sort buffers; endpoints outside [0, n) raise err.
+// 0-based owner/neighbour (+ weight, or the input edge index when eid != 0) into the sort buffers;
+// endpoints outside [0, n) raise err.
 __global__ void k_prepare(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, const uint32_t* __restrict__ w,
                           uint64_t m, uint32_t n, uint32_t shift, uint32_t* __restrict__ key, uint32_t* __restrict__ nb,
-                          uint32_t* __restrict__ wt, uint32_t* __restrict__ err) {
+                          uint32_t* __restrict__ wt, uint32_t* __restrict__ err, int eid) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t s = a[e] - shift, t = b[e] - shift;
         if (s >= n || t >= n) {
@@ -162,7 +163,7 @@ __global__ void k_prepare(const uint32_t* __restrict__ a, const uint32_t* __rest
         }
         key[e] = s;
         nb[e] = t;
-        if (wt) wt[e] = w ? w[e] : 1u;
+        if (wt) wt[e] = eid ? (uint32_t)e : (w ? w[e] : 1u);
     }
 }
 
@@ -305,14 +306,23 @@ __global__ void k_heads(const uint32_t* __restrict__ vstart, uint32_t n, uint32_
 }
 
 // sorted edge i of owner o (rank r = i - rs[o]) goes to slot vstart[o]*K + r: part r/K, lane r%K
+// With veid (edge-index mode) the sorted payload is the input edge index: the weight is gathered from
+// the input array by it and the index is kept per slot.
 __global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __restrict__ nb, const uint32_t* __restrict__ wt,
                         uint64_t m, uint32_t K, const uint32_t* __restrict__ rs, const uint32_t* __restrict__ vstart,
-                        uint32_t* __restrict__ vcol, uint32_t* __restrict__ vw) {
+                        uint32_t* __restrict__ vcol, uint32_t* __restrict__ vw, const uint32_t* __restrict__ w_in,
+                        uint32_t* __restrict__ veid) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t o = key[i];
         const size_t slot = (size_t)vstart[o] * K + (i - rs[o]);
         vcol[slot] = nb[i];
-        if (vw) vw[slot] = wt ? wt[i] : 1u;
+        if (veid) {
+            const uint32_t e = wt[i];
+            veid[slot] = e;
+            if (vw) vw[slot] = w_in ? w_in[e] : 1u;
+        } else if (vw) {
+            vw[slot] = wt ? wt[i] : 1u;
+        }
     }
 }
 
@@ -366,6 +376,8 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     const uint32_t* a = reverse ? d_dst : d_src;
     const uint32_t* b = reverse ? d_src : d_dst;
     const bool with_w = (d_w != nullptr) || (!reverse && vg->weighted);
+    const bool eid = (vg->flags & EEG_VG_EDGE_IDS) != 0;
+    const bool payload = with_w || eid;  // the sort carries a third word: weight, or edge index
 
     EEG_TRY(vg_alloc(vg, (void**)&d->deg, sizeof(uint32_t) * (size_t)(n + 1)));
     EEG_TRY(vg_alloc(vg, (void**)&d->vstart, sizeof(uint32_t) * (size_t)(n + 1)));
@@ -375,7 +387,7 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     for (int i = 0; i < 2; ++i) {
         EEG_TRY(T.get((void**)&key[i], sizeof(uint32_t) * m));
         EEG_TRY(T.get((void**)&nb[i], sizeof(uint32_t) * m));
-        if (with_w) EEG_TRY(T.get((void**)&wt[i], sizeof(uint32_t) * m));
+        if (payload) EEG_TRY(T.get((void**)&wt[i], sizeof(uint32_t) * m));
     }
     EEG_TRY(T.get((void**)&rs, sizeof(uint32_t) * (size_t)(n + 1)));
     EEG_TRY(T.get((void**)&re, sizeof(uint32_t) * (size_t)(n + 1)));
@@ -393,13 +405,13 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     int cur = 0;
     if (m > 0) {
         k_prepare<<<grid_for(m, vg->device), B_TPB, 0, st>>>(a, b, with_w ? d_w : nullptr, m, n, shift, key[0], nb[0],
-                                                              with_w ? wt[0] : nullptr, err);
+                                                              payload ? wt[0] : nullptr, err, eid ? 1 : 0);
         const uint32_t bits = n > 1 ? 32u - (uint32_t)__builtin_clz(n - 1) : 1u;
         for (uint32_t sh = 0; sh < bits; sh += 8) {
             k_radix_hist<<<(unsigned)ntiles, R_TPB, 0, st>>>(key[cur], m, sh, hist, (uint32_t)ntiles);
             EEG_TRY(device_scan_u32(hist, hist, ntiles * R_BINS, false, SCAN_ADD, tmp, st));
             k_radix_scatter<<<(unsigned)ntiles, R_TPB, 0, st>>>(key[cur], nb[cur], wt[cur], key[cur ^ 1], nb[cur ^ 1],
-                                                                with_w ? wt[cur ^ 1] : nullptr, m, sh, hist,
+                                                                payload ? wt[cur ^ 1] : nullptr, m, sh, hist,
                                                                 (uint32_t)ntiles);
             cur ^= 1;
         }
@@ -428,20 +440,23 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     EEG_TRY(vg_alloc(vg, (void**)&d->vowner, sizeof(uint32_t) * (size_t)std::max<uint64_t>(P, 1)));
     EEG_TRY(vg_alloc(vg, (void**)&d->vcol, sizeof(uint32_t) * std::max<size_t>(slots, 4)));
     if (with_w) EEG_TRY(vg_alloc(vg, (void**)&d->vw, sizeof(uint32_t) * std::max<size_t>(slots, 4)));
+    if (eid) EEG_TRY(vg_alloc(vg, (void**)&d->veid, sizeof(uint32_t) * std::max<size_t>(slots, 4)));
 
     if (P > 0) {
         EEG_CUDA(cudaMemsetAsync(d->vowner, 0, sizeof(uint32_t) * (size_t)P, st));
         EEG_CUDA(cudaMemsetAsync(d->vcol, 0xFF, sizeof(uint32_t) * slots, st));
         if (d->vw) EEG_CUDA(cudaMemsetAsync(d->vw, 0, sizeof(uint32_t) * slots, st));
+        if (d->veid) EEG_CUDA(cudaMemsetAsync(d->veid, 0xFF, sizeof(uint32_t) * slots, st));
         k_heads<<<grid_for(n, vg->device), B_TPB, 0, st>>>(d->vstart, n, d->vowner);
         uint32_t* tmp2 = nullptr;
         EEG_TRY(T.get((void**)&tmp2, sizeof(uint32_t) * (size_t)device_scan_tmp_words(P)));
         EEG_TRY(device_scan_u32(d->vowner, d->vowner, P, true, SCAN_MAX, tmp2, st));
-        k_place<<<grid_for(m, vg->device), B_TPB, 0, st>>>(key[cur], nb[cur], with_w ? wt[cur] : nullptr, m, K, rs,
-                                                            d->vstart, d->vcol, d->vw);
+        k_place<<<grid_for(m, vg->device), B_TPB, 0, st>>>(key[cur], nb[cur], payload ? wt[cur] : nullptr, m, K, rs,
+                                                            d->vstart, d->vcol, d->vw, with_w ? d_w : nullptr,
+                                                            d->veid);
     }
     EEG_CUDA(cudaGetLastError());
-    vg->bytes += sizeof(uint32_t) * ((size_t)(n + 1) * 2 + (size_t)P + slots * (with_w ? 2 : 1));
+    vg->bytes += sizeof(uint32_t) * ((size_t)(n + 1) * 2 + (size_t)P + slots * (1 + (with_w ? 1 : 0) + (eid ? 1 : 0)));
     return EEG_OK;
 }
 

@@ -61,6 +61,7 @@ static void free_dir(eeg_vgraph* vg, VDir& d) {
     vg_free(vg, d.vowner);
     vg_free(vg, d.vcol);
     vg_free(vg, d.vw);
+    vg_free(vg, d.veid);
     vg_free(vg, d.deg);
     d = VDir{};
 }

@@ -131,6 +131,22 @@ __device__ __forceinline__ bool grid_barrier(BarrierWords* bw, uint32_t& epoch, 
     return s_ok != 0;
 }
 
+// Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    const float ap = __fsub_rn(s, bp);
+    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
+}
+// (h1,l1) + (h2,l2) -> normalised pair (compensated FP32 summation)
+__device__ __forceinline__ void pair_add(float& h1, float& l1, float h2, float l2) {
+    float s, e;
+    two_sum(h1, h2, s, e);
+    const float t = __fadd_rn(__fadd_rn(l1, l2), e);
+    h1 = __fadd_rn(s, t);
+    l1 = __fsub_rn(t, __fsub_rn(h1, s));
+}
+
 // Exclusive CTA-wide sum scan of one uint32 per thread. `s_warp` needs 33 entries.
 // Returns the exclusive prefix; *total receives the CTA sum (all threads).
 __device__ __forceinline__ uint32_t block_exclusive_sum(uint32_t x, uint32_t* s_warp, uint32_t* total) {

@@ -26,6 +26,7 @@ struct VDir {
     uint32_t* vowner = nullptr;   // P: owning vertex of each part
     uint32_t* vcol = nullptr;     // P*K: neighbour ids (NO_EDGE padding)
     uint32_t* vw = nullptr;       // P*K: weights (uint32; float bits for PageRank weights) or null
+    uint32_t* veid = nullptr;     // P*K: input edge index of each slot (EEG_VG_EDGE_IDS) or null
     uint32_t* deg = nullptr;      // n: degree in this direction
 };
 

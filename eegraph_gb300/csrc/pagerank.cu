@@ -57,21 +57,6 @@ struct PRArgs {
     uint32_t inplace;
 };
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bp = __fsub_rn(s, a);
-    const float ap = __fsub_rn(s, bp);
-    e = __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp));
-}
-// (h1,l1) + (h2,l2) -> normalised pair
-__device__ __forceinline__ void pair_add(float& h1, float& l1, float h2, float l2) {
-    float s, e;
-    two_sum(h1, h2, s, e);
-    const float t = __fadd_rn(__fadd_rn(l1, l2), e);
-    h1 = __fadd_rn(s, t);
-    l1 = __fsub_rn(t, __fsub_rn(h1, s));
-}
-
 __device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, double sum, float xo, uint32_t od, float* cnext,
                                          double& r, double& nrm) {
     const float xn = a.base + a.damping * (float)sum;

@@ -149,7 +149,9 @@ enum {
     EEG_VG_REVERSE = 1u << 0,   /* also build the in-edge (transposed) virtual graph (PageRank pull) */
     EEG_VG_MANAGED = 1u << 1,   /* allocate in managed memory (the --um path) */
     EEG_VG_INPUT_DEVICE = 1u << 2, /* src/dst/weight pointers are device (or managed) pointers */
-    EEG_VG_SHIFT_ONE = 1u << 3  /* subtract 1 from every id while building (1-based input) */
+    EEG_VG_SHIFT_ONE = 1u << 3, /* subtract 1 from every id while building (1-based input) */
+    EEG_VG_EDGE_IDS = 1u << 4   /* keep each slot's input edge index (per-edge results in input order;
+                                   needed by eeg_ppr_create) */
 };
 
 typedef struct eeg_vgraph_info {
@@ -292,6 +294,39 @@ EEG_API eeg_status eeg_run_noalloc(eeg_algo algo, eeg_variant variant, uint32_t 
                                    uint32_t K, const uint32_t* vstart, const uint32_t* vowner, const uint32_t* vcol,
                                    const uint32_t* vw, uint32_t source, uint32_t* dist, void* stream,
                                    uint32_t* iterations);
+
+/* ------------------------------------------------------------------ differentiable personalised PageRank */
+
+/* Personalised PageRank with an implicit adjoint. No counterpart in the reference (its PageRank,
+ * src/pr.cu:3-288, is unweighted, unpersonalised and not differentiable); it is a project-added form.
+ * Model, per column k of row-major n x C arrays, with W_uv = w_uv / s_u the row-normalised raw edge
+ * weights (s_u = sum of u's out-weights; a vertex with s_u == 0 has no out-flow):
+ *     forward   X = (1-d) T + d W^T X            (x_v = (1-d) t_v + d sum_{u->v} W_uv x_u)
+ *     adjoint   L = G + d W L                    (G = dLoss/dX)
+ *     dLoss/dW_uv = d <X_u, L_v>,  dLoss/dw_uv = (dLoss/dW_uv - sum_v' dLoss/dW_uv' W_uv') / s_u,
+ *     dLoss/dT = (1-d) L.
+ * Both solves are Jacobi sweeps in one persistent launch each; the forward pulls over the transposed
+ * graph, the adjoint over the forward graph (no atomics, no transpose at run time, no iterate storage).
+ * FP32 values and accumulation; the stop test d/(1-d)*||Y_{k+1}-Y_k||_1 <= tol*||Y_{k+1}||_1 (all columns
+ * together, eeg_options.pr_tolerance, default 1e-7) is reduced in FP64. C = 1 runs the single-column
+ * kernels (the plain form); 2 <= C <= 64 runs the batched row kernels (rows padded to 64 columns). */
+typedef struct eeg_ppr eeg_ppr;
+/* vg must be built with EEG_VG_REVERSE | EEG_VG_EDGE_IDS and outlive the handle. */
+EEG_API eeg_status eeg_ppr_create(eeg_vgraph* vg, uint32_t columns, eeg_ppr** out);
+/* Raw edge weights w[num_edges] in input edge order (finite, >= 0), host or device memory. */
+EEG_API eeg_status eeg_ppr_set_weights(eeg_ppr* p, const float* w, int on_device);
+/* Forward solve. teleport: n x C (host, or device with in_on_device). x_out (may be NULL): n x C.
+ * X is kept for the next eeg_ppr_adjoint. */
+EEG_API eeg_status eeg_ppr_forward(eeg_ppr* p, const float* teleport, int in_on_device, float* x_out,
+                                   int out_on_device, const eeg_options* opts, void* stream, eeg_result* res);
+/* Adjoint solve for dl_dx (n x C) and the gradients, each output optional (NULL): dl_dteleport n x C,
+ * dl_dw[num_edges] and dl_dwn[num_edges] (w.r.t. the raw and the normalised weights, input edge order).
+ * accumulate != 0 adds the edge gradients to those of earlier adjoint calls on this handle (so a loop of
+ * single-column calls returns the sum over columns); dl_dteleport is never accumulated. */
+EEG_API eeg_status eeg_ppr_adjoint(eeg_ppr* p, const float* dl_dx, int in_on_device, float* dl_dteleport,
+                                   float* dl_dw, float* dl_dwn, int out_on_device, int accumulate,
+                                   const eeg_options* opts, void* stream, eeg_result* res);
+EEG_API void eeg_ppr_destroy(eeg_ppr* p);
 
 /* ------------------------------------------------------------------ energy (NVML) */
 

@@ -67,6 +67,10 @@ def lib():
         _o.orc_cc_labels.argtypes = [u32, u64, vp, vp, vp, vp]
         _o.orc_pagerank.restype = C.c_int64
         _o.orc_pagerank.argtypes = [u32, u64, vp, vp, C.c_double, C.c_double, u64, vp]
+        _o.orc_ppr_solve.restype = C.c_int64
+        _o.orc_ppr_solve.argtypes = [u32, u64, vp, vp, vp, u32, vp, C.c_double, C.c_int, C.c_double, C.c_double,
+                                     u64, vp]
+        _o.orc_ppr_grads.argtypes = [u32, u64, vp, vp, vp, u32, vp, vp, C.c_double, vp, vp, vp]
     return _o
 
 
@@ -176,6 +180,49 @@ def pagerank(n, src, dst, damping=0.85, tol=1e-15, max_iter=100000):
     src, dst = _u32(src), _u32(dst)
     it = lib().orc_pagerank(n, src.size, _vp(src), _vp(dst), damping, tol, max_iter, _vp(x))
     return x, it
+
+
+def _f64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a if shape is None else a.reshape(shape)
+
+
+def ppr_solve(n, src, dst, w, b, transpose=False, damping=0.85, tol=1e-14, max_iter=100000):
+    """FP64 personalised PageRank (transpose=False: X = (1-d)B + d W^T X) or its adjoint
+    (transpose=True: L = B + d W L) on row-normalised weights; b is n x C. Returns (Y, sweeps)."""
+    src, dst, w = _u32(src), _u32(dst), _f64(w)
+    b = _f64(b)
+    if b.ndim == 1:
+        b = b.reshape(n, 1)
+    C_ = b.shape[1]
+    y = np.empty((n, C_), np.float64)
+    scale = 1.0 if transpose else 1.0 - damping
+    it = lib().orc_ppr_solve(n, src.size, _vp(src), _vp(dst), _vp(w), C_, _vp(b), scale, int(transpose), damping,
+                             tol, max_iter, _vp(y))
+    if it < 0:
+        raise RuntimeError("oracle PPR solve did not converge")
+    return y, it
+
+
+def ppr_grads(n, src, dst, w, X, L, damping=0.85):
+    """(dLoss/dW_normalised per edge, dLoss/dw_raw per edge, dLoss/dT) from X and the adjoint L."""
+    src, dst, w = _u32(src), _u32(dst), _f64(w)
+    X, L = _f64(X), _f64(L)
+    C_ = X.shape[1]
+    m = src.size
+    gWn = np.empty(m, np.float64)
+    gw = np.empty(m, np.float64)
+    gT = np.empty_like(L)
+    lib().orc_ppr_grads(n, m, _vp(src), _vp(dst), _vp(w), C_, _vp(X), _vp(L), damping, _vp(gWn), _vp(gw), _vp(gT))
+    return gWn, gw, gT
+
+
+def ppr(n, src, dst, w, T, G, damping=0.85, tol=1e-14):
+    """Forward, adjoint and gradients in FP64. T: teleport (n x C), G: dLoss/dX (n x C)."""
+    X, itf = ppr_solve(n, src, dst, w, T, False, damping, tol)
+    L, ita = ppr_solve(n, src, dst, w, G, True, damping, tol)
+    gWn, gw, gT = ppr_grads(n, src, dst, w, X, L, damping)
+    return {"X": X, "L": L, "gWn": gWn, "gw": gw, "gT": gT, "sweeps": (itf, ita)}
 
 
 def expected(algo, variant, n, src, dst, w, source):

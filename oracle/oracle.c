@@ -4,6 +4,7 @@
  */
 #include "oracle.h"
 
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -465,4 +466,73 @@ int64_t orc_pagerank(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t
     free(y);
     free(c);
     return it;
+}
+
+/* ------------------------------------------------------------------ personalised PageRank (FP64) */
+static double* orc_out_sums(uint32_t n, uint64_t m, const uint32_t* src, const double* w) {
+    double* s = (double*)calloc(n ? n : 1, sizeof(double));
+    for (uint64_t e = 0; e < m; ++e) s[src[e]] += w[e];
+    return s;
+}
+
+int64_t orc_ppr_solve(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
+                      const double* b, double scale_b, int transpose, double damping, double tol, uint64_t max_iter,
+                      double* y) {
+    const size_t N = (size_t)n * C;
+    double* s = orc_out_sums(n, m, src, w);
+    double* z = (double*)malloc((N ? N : 1) * sizeof(double));
+    for (size_t i = 0; i < N; ++i) y[i] = scale_b * b[i];
+    int64_t it = 0;
+    int converged = 0;
+    while ((uint64_t)it < max_iter) {
+        ++it;
+        for (size_t i = 0; i < N; ++i) z[i] = scale_b * b[i];
+        for (uint64_t e = 0; e < m; ++e) {
+            const uint32_t u = src[e], v = dst[e];
+            if (s[u] == 0.0) continue;
+            const double a = damping * (w[e] / s[u]);
+            /* forward pushes u's row into v; the adjoint pulls v's row into u */
+            const uint32_t from = transpose ? v : u, to = transpose ? u : v;
+            const double* yr = y + (size_t)from * C;
+            double* zr = z + (size_t)to * C;
+            for (uint32_t k = 0; k < C; ++k) zr[k] += a * yr[k];
+        }
+        double diff = 0.0, norm = 0.0;
+        for (size_t i = 0; i < N; ++i) {
+            diff += fabs(z[i] - y[i]);
+            norm += fabs(z[i]);
+            y[i] = z[i];
+        }
+        if (damping / (1.0 - damping) * diff <= tol * norm) {
+            converged = 1;
+            break;
+        }
+    }
+    free(z);
+    free(s);
+    return converged ? it : -1;
+}
+
+void orc_ppr_grads(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
+                   const double* X, const double* L, double damping, double* gWn, double* gw, double* gT) {
+    double* s = orc_out_sums(n, m, src, w);
+    double* g = (double*)malloc((m ? m : 1) * sizeof(double));
+    double* r = (double*)calloc(n ? n : 1, sizeof(double));
+    for (uint64_t e = 0; e < m; ++e) {
+        const double* xr = X + (size_t)src[e] * C;
+        const double* lr = L + (size_t)dst[e] * C;
+        double dot = 0.0;
+        for (uint32_t k = 0; k < C; ++k) dot += xr[k] * lr[k];
+        g[e] = damping * dot;
+        if (s[src[e]] != 0.0) r[src[e]] += g[e] * (w[e] / s[src[e]]);
+    }
+    for (uint64_t e = 0; e < m; ++e) {
+        if (gWn) gWn[e] = g[e];
+        if (gw) gw[e] = s[src[e]] != 0.0 ? (g[e] - r[src[e]]) / s[src[e]] : 0.0;
+    }
+    if (gT)
+        for (size_t i = 0; i < (size_t)n * C; ++i) gT[i] = (1.0 - damping) * L[i];
+    free(r);
+    free(g);
+    free(s);
 }

@@ -11,6 +11,9 @@
  *                                                                 src/eegraph.cu:89-211
  *   orc_dijkstra / orc_bfs / orc_widest / orc_pagerank: independent textbook algorithms that pin the
  *   fixed points (Dijkstra 1959; breadth-first search; max-min Dijkstra; power iteration in FP64).
+ *   orc_ppr_*: FP64 personalised PageRank on row-normalised edge weights, its adjoint solve and the
+ *   gradients (a project-added form: the reference has no counterpart, so these pin the GPU kernels
+ *   by mathematics -- finite differences and the duality c^T x = (1-d) t^T lambda are checked in tests).
  * Parity pinned against the reference itself: oracle/_ref (built from the reference sources) and the
  * golden vectors in tests/golden/ that it produced.
  */
@@ -66,6 +69,21 @@ void orc_cc_labels(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* 
  * ||x_{k+1}-x_k||_1 <= tol * ||x||_1. Returns iterations. */
 int64_t orc_pagerank(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, double damping, double tol,
                      uint64_t max_iter, double* x);
+
+/* Personalised PageRank on row-normalised weights W_e = w_e / s_src(e), s_u = sum of w over u's
+ * out-edges (W = 0 where s_u == 0). C columns, row-major n x C arrays.
+ *   forward : X = (1-d) T + d W^T X        (x_v = (1-d) t_v + d sum_{e: u->v} W_e x_u)
+ *   adjoint : L = G + d W L                (l_u = g_u + d sum_{e: u->v} W_e l_v), G = dLoss/dX
+ * Jacobi in FP64 until d/(1-d) * ||Y_{k+1}-Y_k||_1 <= tol * ||Y_{k+1}||_1 (all columns together).
+ * Returns the sweeps taken, or -1 when max_iter was reached first. */
+int64_t orc_ppr_solve(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
+                      const double* b, double scale_b, int transpose, double damping, double tol, uint64_t max_iter,
+                      double* y);
+/* Gradients from X and L: gWn_e = d <X_src(e), L_dst(e)> (w.r.t. the normalised weight),
+ * gw_e = (gWn_e - sum_{e' out of src(e)} gWn_e' W_e') / s_src(e) (w.r.t. the raw weight; 0 where s == 0),
+ * gT = (1-d) L. Any output may be NULL. */
+void orc_ppr_grads(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
+                   const double* X, const double* L, double damping, double* gWn, double* gw, double* gT);
 
 #ifdef __cplusplus
 }

@@ -106,3 +106,43 @@ def test_restatement_matches_reference_library(seed):
     for algo in ("bfs", "sssp", "sswp", "cc"):
         got, _ = oracle.seq_sweep(algo, n, s, d, w, src, K=8, wrap=True)
         assert np.array_equal(got, oracle.ref_seq_cpu(algo, n, s, d, w, src))
+
+
+def test_ppr_oracle_adjoint_against_finite_differences():
+    """FP64 personalised PageRank oracle: adjoint gradients equal central differences; duality
+    c^T x = (1-d) t^T lambda; sum_v w_uv dL/dw_uv = 0 per source (row normalisation is scale-free)."""
+    rng = np.random.default_rng(3)
+    n, m, C = 60, 400, 3
+    src = rng.integers(0, n, m).astype(np.uint32)
+    dst = rng.integers(0, n, m).astype(np.uint32)
+    src[:5] = 7  # a few parallel edges and a vertex with several out-edges
+    dst[:5] = 9
+    w = rng.uniform(0.01, 1.0, m)
+    T = np.zeros((n, C))
+    for k in range(C):
+        T[rng.choice(n, 6, replace=False), k] = 1 / 6
+    G = rng.standard_normal((n, C))
+    r = oracle.ppr(n, src, dst, w, T, G)
+    assert abs((G * r["X"]).sum() - 0.15 * (T * r["L"]).sum()) <= 1e-12 * np.abs(G * r["X"]).sum()
+
+    def loss(wv, Tv):
+        return (G * oracle.ppr_solve(n, src, dst, wv, Tv)[0]).sum()
+
+    eps = 1e-6
+    for e in (0, 3, 100, 399):
+        wp, wm = w.copy(), w.copy()
+        wp[e] += eps
+        wm[e] -= eps
+        fd = (loss(wp, T) - loss(wm, T)) / (2 * eps)
+        assert abs(fd - r["gw"][e]) <= 1e-7 + 1e-6 * abs(r["gw"][e])
+    for i, k in ((0, 0), (13, 2), (59, 1)):
+        Tp, Tm = T.copy(), T.copy()
+        Tp[i, k] += eps
+        Tm[i, k] -= eps
+        fd = (loss(w, Tp) - loss(w, Tm)) / (2 * eps)
+        assert abs(fd - r["gT"][i, k]) <= 1e-7 + 1e-6 * abs(r["gT"][i, k])
+    tot = np.zeros(n)
+    np.add.at(tot, src, w * r["gw"])
+    assert np.abs(tot).max() <= 1e-12
+    # normalised-weight gradient: d <x_u, lambda_v>
+    assert np.allclose(r["gWn"], 0.85 * (r["X"][src] * r["L"][dst]).sum(1), rtol=1e-12, atol=1e-15)
