@@ -41,10 +41,10 @@ ALGO_PLAN = [("bfs", "sync_push_dd"), ("sssp", "sync_push_dd"), ("sswp", "sync_p
 PR_TOL = 1e-7
 
 
-def workload_name(scale: int, K: int) -> str:
+def workload_name(scale: int, K: int, pr_k: int = 16) -> str:
     return (f"R-MAT s{scale} ef{EF} a/b/c/d=.57/.19/.19/.05 seed {SEED} w~U[1,63]; BFS/SSSP/SSWP sync_push_dd "
             f"from max-out-degree vertex, CC async_push_dd on the symmetrised graph, PR sync_push_td d=0.85 "
-            f"tol 1e-7; K={K}")
+            f"tol 1e-7; K={K} (PageRank's transposed graph K={pr_k})")
 
 
 def dist_env():
@@ -161,9 +161,9 @@ def teps_edges(algo: str, res: dict, m: int, m_sym: int) -> float:
     return float(res["reached_edges"])
 
 
-def run_step(vg, vg_sym, source, outs, stream, results):
+def run_step(vg, vg_sym, vg_pr, source, outs, stream, results):
     for algo, variant in ALGO_PLAN:
-        g = vg_sym if algo == "cc" else vg
+        g = vg_sym if algo == "cc" else (vg_pr if algo == "pr" else vg)
         _, res = g.run(algo, variant, source, out_device_ptr=outs[algo], stream=stream,
                        pr_tolerance=PR_TOL)
         results[algo] = res
@@ -187,8 +187,10 @@ def bench_gpu(args) -> None:
     m, m_sym = s.size, ss.size
     stream = torch.cuda.current_stream(dev).cuda_stream
 
-    vg = E.VirtualGraph.build(n, s, d, w, K=args.k, reverse=True, stream=stream)
+    vg = E.VirtualGraph.build(n, s, d, w, K=args.k, stream=stream)
     vg_sym = E.VirtualGraph.build(n, ss, ds, ws, K=args.k, stream=stream)
+    # PageRank pulls over the transposed graph: its own part size (unweighted)
+    vg_pr = E.VirtualGraph.build(n, s, d, None, K=args.pr_k, reverse=True, stream=stream)
     info = vg.info()
     source = info["max_degree_vertex"]
     outs_t = {a: torch.empty(n, dtype=torch.int32, device=dev) for a, _ in ALGO_PLAN}
@@ -197,7 +199,7 @@ def bench_gpu(args) -> None:
 
     results: dict = {}
     for _ in range(args.warmup):
-        run_step(vg, vg_sym, source, outs, stream, results)
+        run_step(vg, vg_sym, vg_pr, source, outs, stream, results)
     torch.cuda.synchronize()
 
     per_algo = {a: {"ms": [], "edges": [], "bytes": [], "iters": []} for a, _ in ALGO_PLAN}
@@ -212,7 +214,7 @@ def bench_gpu(args) -> None:
         for i in range(args.steps):
             flush.fill_(float(i))  # L2 flush between timed steps (outside the events)
             starts[i].record()
-            run_step(vg, vg_sym, source, outs, stream, results)
+            run_step(vg, vg_sym, vg_pr, source, outs, stream, results)
             ends[i].record()
             for a, _ in ALGO_PLAN:
                 r = results[a]
@@ -241,14 +243,16 @@ def bench_gpu(args) -> None:
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        g1 = E.VirtualGraph.build(n, pin["s"], pin["d"], pin["w"], K=args.k, reverse=True, stream=stream)
+        g1 = E.VirtualGraph.build(n, pin["s"], pin["d"], pin["w"], K=args.k, stream=stream)
         g2 = E.VirtualGraph.build(n, pin["ss"], pin["ds"], pin["ws"], K=args.k, stream=stream)
+        g3 = E.VirtualGraph.build(n, pin["s"], pin["d"], None, K=args.pr_k, reverse=True, stream=stream)
         src_e2e = g1.info()["max_degree_vertex"]
         for algo, variant in ALGO_PLAN:
-            (g2 if algo == "cc" else g1).run(algo, variant, src_e2e, out=host_out[algo], stream=stream,
-                                             pr_tolerance=PR_TOL)
+            (g2 if algo == "cc" else (g3 if algo == "pr" else g1)).run(algo, variant, src_e2e, out=host_out[algo],
+                                                                        stream=stream, pr_tolerance=PR_TOL)
         g1.close()
         g2.close()
+        g3.close()
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
@@ -258,7 +262,7 @@ def bench_gpu(args) -> None:
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_total_ms = float(tt[0])
     e2e_value = total_edges_all / (e2e_total_ms * 1e-3) / 1e9 if e2e_ms else None
-    h2d = 4 * (3 * m + 3 * m_sym)
+    h2d = 4 * (3 * m + 3 * m_sym + 2 * m)
     d2h = 4 * n * len(ALGO_PLAN)
 
     if rank != 0:
@@ -280,7 +284,7 @@ def bench_gpu(args) -> None:
     dom = max(algo_summary, key=lambda a: algo_summary[a]["kernel_ms"])
     kern_name = {"bfs": "k_traverse<OP_BFS>", "sssp": "k_traverse<OP_SSSP>", "sswp": "k_traverse<OP_SSWP>",
                  "cc": "k_traverse<OP_CC>", "pr": "k_pagerank"}[dom]
-    wl = workload_name(scale, args.k)
+    wl = workload_name(scale, args.k, args.pr_k)
     ach = algo_summary[dom]["achieved_GBs"]
     line = {
         "metric": "GTEPS (sum over BFS,SSSP,SSWP,CC,PR of TEPS edges / device time)",
@@ -295,13 +299,14 @@ def bench_gpu(args) -> None:
         "vs_baseline": None,
         "dtype": "u32 (BFS/SSSP/SSWP/CC), f32 (PageRank)",
         "data": "synthetic (seeded R-MAT, generated in-process)",
-        "config": {"workload": wl, "scale": scale, "edge_factor": EF, "K": args.k, "vertices": n, "edges": m,
+        "config": {"workload": wl, "scale": scale, "edge_factor": EF, "K": args.k, "pr_K": args.pr_k,
+                   "vertices": n, "edges": m,
                    "cc_arcs": m_sym, "source": source, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (part arrays ~0.7 GB) and 256 MB L2 flush between timed steps"},
         "per_algo": algo_summary,
         "roofline": {"bound": "hbm", "kernel": kern_name, "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                     "traffic": load_traffic(kern_name, f"s{scale}_k{args.k}")},
+                     "traffic": load_traffic(kern_name, f"s{scale}_k{args.pr_k if dom == 'pr' else args.k}")},
         "e2e": {"value": round(e2e_value, 3) if e2e_value else None, "unit": "GTEPS", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_total_ms / args.steps, 3)},
         "gpu_launches": launches,
@@ -709,6 +714,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--k", type=int, default=8, choices=[4, 8, 16])
+    ap.add_argument("--pr-k", type=int, default=16, choices=[4, 8, 16],
+                    help="part size of PageRank's graph (pull over the transposed graph)")
     ap.add_argument("--scale", type=int, default=SCALE)
     ap.add_argument("--cpu-budget", type=float, default=30.0)
     ap.add_argument("--cpu-threads", type=int, default=0)

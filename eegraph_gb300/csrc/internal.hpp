@@ -68,6 +68,8 @@ struct Workspace {
     float* contrib[2] = {nullptr, nullptr};  // n each
     double* acc = nullptr;        // n (partials of vertices whose parts cross warp chunks)
     uint32_t* arrive = nullptr;   // n (chunks that delivered a partial, per vertex)
+    uint32_t* pr_rank = nullptr;  // n (+ class counters): rank of each vertex by out-degree class
+    uint32_t* pr_rcol = nullptr;  // transposed graph's neighbour ids as ranks (P_rev * K)
     PRCtrl* pctrl = nullptr;
     // misc
     unsigned long long* stats = nullptr;  // reached counters

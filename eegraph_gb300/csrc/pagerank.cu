@@ -11,8 +11,8 @@
 //    (256-bit loads) and then all 2*K gathers of contrib[u] = x_u / outdeg(u) are issued before any
 //    of them is consumed; the old value and out-degree of each chunk's segment ends are prefetched
 //    alongside the gathers.
-//  * Each lane sums its part with a compensated (two-sum) FP32 accumulation; parts of one vertex are
-//    combined by a segmented warp scan of (hi, lo) pairs.
+//  * Each lane sums its part's K values by a pairwise tree; parts of one vertex are combined by a
+//    segmented warp scan of compensated (hi, lo) pairs.
 //  * A vertex whose parts all sit in one chunk is finalised in place. A vertex whose parts span chunks
 //    gets one FP64 atomic partial per chunk plus an arrival count; the warp that brings the count to
 //    the number of chunks spanned finalises it. So a sweep needs ONE grid barrier.
@@ -29,7 +29,8 @@
 namespace eeg {
 namespace {
 
-constexpr int PR_TPB = 512;
+constexpr int PR_TPB = 1024;  // one CTA per SM: its shared memory holds the hot contributions
+constexpr uint32_t PR_HOT_DEFAULT = 32768;
 // chunks in flight per warp (K = 16 keeps one: its 16 ids + 16 gathered values already fill the registers)
 template <int K>
 struct InFlight {
@@ -41,8 +42,10 @@ struct PRArgs {
     uint32_t RP;
     const uint32_t* __restrict__ rvstart;
     const uint32_t* __restrict__ rvowner;
-    const uint32_t* __restrict__ rvcol;
+    const uint32_t* __restrict__ rvcol;   // transposed graph's neighbours, as ranks (see rank below)
     const uint32_t* __restrict__ outdeg;
+    const uint32_t* __restrict__ rank;    // position of each vertex in descending out-degree-class order
+    uint32_t hot;                         // contributions of ranks < hot are staged in shared memory
     float* x;
     float* c0;
     float* c1;
@@ -57,13 +60,13 @@ struct PRArgs {
     uint32_t inplace;
 };
 
-__device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, double sum, float xo, uint32_t od, float* cnext,
-                                         double& r, double& nrm) {
+__device__ __forceinline__ void finalize(const PRArgs& a, uint32_t v, uint32_t rk, double sum, float xo, uint32_t od,
+                                         float* cnext, double& r, double& nrm) {
     const float xn = a.base + a.damping * (float)sum;
     r += fabs((double)xn - (double)xo);
     nrm += (double)xn;
     a.x[v] = xn;
-    cnext[v] = od ? xn / (float)od : 0.f;
+    cnext[rk] = od ? xn / (float)od : 0.f;
 }
 
 constexpr int XCAP = 64;  // per-warp list of (vertex, chunks spanned) awaiting their arrival count
@@ -89,8 +92,10 @@ __device__ __forceinline__ void settle_spanning(const PRArgs& a, const uint2* xb
 }
 
 template <int K>
-__global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
+__global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
     constexpr int PR_U = InFlight<K>::U;
+    extern __shared__ float4 s_hot4[];  // contributions of the `hot` highest out-degree vertices
+    const float* s_hot = reinterpret_cast<const float*>(s_hot4);
     __shared__ double s_red[2][PR_TPB / 32];
     __shared__ unsigned long long s_zero;
     __shared__ uint2 s_span[PR_TPB / 32][XCAP];
@@ -112,8 +117,9 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
         a.x[v] = a.base;
         const uint32_t od = a.outdeg[v];
         const float c = od ? a.base / (float)od : 0.f;
-        a.c0[v] = c;
-        a.c1[v] = c;
+        const uint32_t rk = a.rank[v];
+        a.c0[rk] = c;
+        a.c1[rk] = c;
         a.acc[v] = 0.0;
         a.arrive[v] = 0u;
         zero_in += (a.rvstart[v + 1] == a.rvstart[v]) ? 1ull : 0ull;
@@ -146,59 +152,72 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
             double r = 0.0, nrm = 0.0;
             uint32_t nx = 0;  // warp-uniform fill of xbuf
             auto fin = [&](uint32_t vv, double sum) {
-                finalize(a, vv, sum, __ldcg(&a.x[vv]), __ldg(&a.outdeg[vv]), cnext, r, nrm);
+                finalize(a, vv, __ldg(&a.rank[vv]), sum, __ldcg(&a.x[vv]), __ldg(&a.outdeg[vv]), cnext, r, nrm);
             };
+            // stage this sweep's hot contributions (the barrier before the sweep ordered every CTA's
+            // writes of the previous sweep; ASYNC may see some of this sweep's, which it allows)
+            {
+                const float4* src4 = reinterpret_cast<const float4*>(ccur);
+                for (uint32_t i = threadIdx.x; i < a.hot / 4u; i += PR_TPB) s_hot4[i] = src4[i];
+                __syncthreads();
+            }
 
             for (uint32_t base = gwarp; base < nchunks; base += nwarps * PR_U) {
-                uint32_t v[PR_U], col[PR_U][K];
+                uint32_t v[PR_U], col[PR_U][K], vb[PR_U];
                 bool valid[PR_U];
 #pragma unroll
                 for (int u = 0; u < PR_U; ++u) {
                     const uint32_t ch = base + (uint32_t)u * nwarps;
                     const uint32_t p = ch * 32u + lane;
                     valid[u] = ch < nchunks && p < a.RP;
-                    v[u] = 0xFFFFFFFFu;
+                    v[u] = vb[u] = 0xFFFFFFFFu;
                     if (valid[u]) {
                         v[u] = __ldg(&a.rvowner[p]);
                         ld_part<K>(a.rvcol + (size_t)p * K, col[u], pol);
+                        // owners just outside the chunk: lane 0 the part before it, lane 31 the part after
+                        if (lane == 0u && p > 0u) vb[u] = __ldg(&a.rvowner[p - 1u]);
+                        if (lane == 31u && p + 1u < a.RP) vb[u] = __ldg(&a.rvowner[p + 1u]);
                     }
                 }
+                // padding slots gather 0 (adding an exact zero leaves the compensated sum unchanged),
+                // so the id registers die here
                 float y[PR_U][K];
+                uint32_t nvalid = 0;
 #pragma unroll
                 for (int u = 0; u < PR_U; ++u)
 #pragma unroll
-                    for (int i = 0; i < K; ++i)
-                        y[u][i] = (valid[u] && col[u][i] != NO_EDGE) ? ccur[col[u][i]] : 0.f;
+                    for (int i = 0; i < K; ++i) {
+                        const bool ok = valid[u] && col[u][i] != NO_EDGE;
+                        nvalid += ok ? 1u : 0u;
+                        y[u][i] = ok ? (col[u][i] < a.hot ? s_hot[col[u][i]] : ccur[col[u][i]]) : 0.f;
+                    }
+                my_edges += nvalid;
                 // segment ends: prefetch what finalisation needs while the gathers are in flight
                 bool last[PR_U];
                 float xo[PR_U];
-                uint32_t od[PR_U], vs0[PR_U], vs1[PR_U];
+                uint32_t od[PR_U], rk[PR_U];
 #pragma unroll
                 for (int u = 0; u < PR_U; ++u) {
                     const uint32_t vn = __shfl_down_sync(0xffffffffu, v[u], 1);
                     last[u] = valid[u] && (lane == 31u || vn != v[u]);
                     xo[u] = 0.f;
                     od[u] = 0u;
-                    vs0[u] = vs1[u] = 0u;
+                    rk[u] = 0u;
                     if (last[u]) {
+                        rk[u] = __ldg(&a.rank[v[u]]);
                         xo[u] = __ldcg(&a.x[v[u]]);
                         od[u] = __ldg(&a.outdeg[v[u]]);
-                        vs0[u] = __ldg(&a.rvstart[v[u]]);
-                        vs1[u] = __ldg(&a.rvstart[v[u] + 1]);
                     }
                 }
 #pragma unroll
                 for (int u = 0; u < PR_U; ++u) {
-                    float hi = 0.f, lo = 0.f;
+                    // the part's K values by a pairwise tree (rounding error <= log2(K) ulps of the
+                    // part sum); parts and chunks are then combined with compensation
 #pragma unroll
-                    for (int i = 0; i < K; ++i) {
-                        if (!valid[u] || col[u][i] == NO_EDGE) break;
-                        ++my_edges;
-                        float t, e;
-                        two_sum(hi, y[u][i], t, e);
-                        hi = t;
-                        lo = __fadd_rn(lo, e);
-                    }
+                    for (int w = K / 2; w >= 1; w >>= 1)
+#pragma unroll
+                        for (int i = 0; i < w; ++i) y[u][i] = __fadd_rn(y[u][i], y[u][i + w]);
+                    float hi = y[u][0], lo = 0.f;
                     // segmented inclusive scan over lanes of the same vertex (a vertex's parts are contiguous):
                     // segment heads from one shuffle + ballot, and only as many steps as the longest segment
                     const uint32_t vprev = __shfl_up_sync(0xffffffffu, v[u], 1);
@@ -212,15 +231,15 @@ __global__ void __launch_bounds__(PR_TPB, 2) k_pagerank(PRArgs a) {
                     }
                     bool spans = false;
                     uint32_t need = 0;
+                    const uint32_t before0 = __shfl_sync(0xffffffffu, vb[u], 0);
                     if (last[u]) {
-                        const uint32_t ch = base + (uint32_t)u * nwarps;
-                        const uint32_t first_chunk = vs0[u] / 32u, last_chunk = (vs1[u] - 1u) / 32u;
-                        if (first_chunk == ch && last_chunk == ch) {
-                            finalize(a, v[u], (double)hi + (double)lo, xo[u], od[u], cnext, r, nrm);
+                        // the vertex began before this chunk, or continues after it
+                        if (!((seg0 == 0u && before0 == v[u]) || (lane == 31u && vb[u] == v[u]))) {
+                            finalize(a, v[u], rk[u], (double)hi + (double)lo, xo[u], od[u], cnext, r, nrm);
                         } else {  // partial now, arrival counted in the warp's next settle
                             atomicAdd(&a.acc[v[u]], (double)hi + (double)lo);
                             spans = true;
-                            need = last_chunk - first_chunk + 1u;
+                            need = (__ldg(&a.rvstart[v[u] + 1]) - 1u) / 32u - __ldg(&a.rvstart[v[u]]) / 32u + 1u;
                         }
                     }
                     const uint32_t m = __ballot_sync(0xffffffffu, spans);
@@ -277,10 +296,24 @@ finish:
 }
 
 template <int K>
-eeg_status launch_pr(const PRArgs& args, int device, uint32_t bps, cudaStream_t st) {
+eeg_status launch_pr(const PRArgs& args, int device, uint32_t bps, uint32_t hot_limit, cudaStream_t st) {
     auto kern = k_pagerank<K>;
+    // shared memory left after the static arrays holds the hot contributions (multiple of 4 floats)
+    cudaFuncAttributes fa{};
+    EEG_CUDA(cudaFuncGetAttributes(&fa, kern));
+    int optin = 0;
+    EEG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    const size_t room = optin > (int)fa.sharedSizeBytes + 1024 ? (size_t)optin - fa.sharedSizeBytes - 1024 : 0;
+    PRArgs a = args;
+    // default 32K vertices (128 KB): a larger carve-out shrinks L1 below what the cold gathers and the
+    // per-vertex loads need (measured on R-MAT s22: 128 KB best, 210 KB 35 % slower than none)
+    size_t hot = std::min<size_t>(args.n, room / sizeof(float));
+    hot = std::min<size_t>(hot, hot_limit ? hot_limit : PR_HOT_DEFAULT);
+    a.hot = (uint32_t)(hot & ~(size_t)3);
+    const size_t dyn = (size_t)a.hot * sizeof(float);
+    EEG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
     int per_sm = 0;
-    EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PR_TPB, 0));
+    EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PR_TPB, dyn));
     if (per_sm <= 0) {
         set_last_error("pagerank kernel does not fit on an SM");
         return EEG_ERR_CUDA;
@@ -290,10 +323,78 @@ eeg_status launch_pr(const PRArgs& args, int device, uint32_t bps, cudaStream_t 
     const uint64_t work = std::max<uint64_t>(args.RP, args.n);
     const uint64_t need = (work + PR_TPB - 1) / PR_TPB;
     if (need < blocks) blocks = std::max<uint64_t>(need, 1);
-    PRArgs a = args;
     void* params[] = {(void*)&a};
-    EEG_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)blocks), dim3(PR_TPB), params, 0, st));
+    EEG_CUDA(cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)blocks), dim3(PR_TPB), params, dyn, st));
     return EEG_OK;
+}
+
+// ---- degree-class relabelling of the transposed graph's neighbour ids (once per graph)
+constexpr uint32_t RCLS = 129;  // quarter-octave out-degree classes, descending; class 128 = no out-edges
+constexpr uint32_t RTILE = 4096;
+
+__device__ __forceinline__ uint32_t deg_class(uint32_t d) {
+    if (d == 0) return RCLS - 1;
+    const uint32_t lg = 31u - __clz(d);
+    const uint32_t frac = lg >= 2 ? (d >> (lg - 2)) & 3u : (d << (2 - lg)) & 3u;
+    return 127u - (lg * 4u + frac);
+}
+
+__global__ void k_rank_hist(uint32_t n, const uint32_t* __restrict__ deg, uint32_t* hist) {
+    __shared__ uint32_t sh[RCLS];
+    for (uint32_t i = threadIdx.x; i < RCLS; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        atomicAdd(&sh[deg_class(deg[v])], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < RCLS; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], sh[i]);
+}
+// hist -> exclusive class offsets (in place), cursors zeroed
+__global__ void k_rank_base(uint32_t* hist, uint32_t* cursor) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t i = 0; i < RCLS; ++i) {
+            const uint32_t c = hist[i];
+            hist[i] = run;
+            run += c;
+            cursor[i] = 0;
+        }
+    }
+}
+// rank[v] = class offset + a slot reserved per CTA and class (order within a class is not fixed;
+// results do not depend on it)
+__global__ void k_rank_scatter(uint32_t n, const uint32_t* __restrict__ deg, const uint32_t* __restrict__ base,
+                               uint32_t* cursor, uint32_t* rank) {
+    __shared__ uint32_t s_cnt[RCLS], s_off[RCLS];
+    for (uint64_t t0 = (uint64_t)blockIdx.x * RTILE; t0 < n; t0 += (uint64_t)gridDim.x * RTILE) {
+        for (uint32_t i = threadIdx.x; i < RCLS; i += blockDim.x) s_cnt[i] = 0;
+        __syncthreads();
+        constexpr int PER = RTILE / 256;
+        uint32_t cls[PER], loc[PER];
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const uint64_t v = t0 + (uint64_t)j * blockDim.x + threadIdx.x;
+            cls[j] = v < n ? deg_class(deg[v]) : RCLS;
+            loc[j] = v < n ? atomicAdd(&s_cnt[cls[j]], 1u) : 0u;
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < RCLS; i += blockDim.x)
+            s_off[i] = s_cnt[i] ? base[i] + atomicAdd(&cursor[i], s_cnt[i]) : 0u;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PER; ++j) {
+            const uint64_t v = t0 + (uint64_t)j * blockDim.x + threadIdx.x;
+            if (v < n) rank[v] = s_off[cls[j]] + loc[j];
+        }
+        __syncthreads();
+    }
+}
+__global__ void k_rank_cols(uint64_t slots, const uint32_t* __restrict__ col, const uint32_t* __restrict__ rank,
+                            uint32_t* __restrict__ out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = col[i];
+        out[i] = c == NO_EDGE ? NO_EDGE : rank[c];
+    }
 }
 
 }  // namespace
@@ -314,6 +415,32 @@ static eeg_status ensure_pr_ws(eeg_vgraph* vg) {
     return EEG_OK;
 }
 
+// Ranks by descending out-degree class and the transposed graph's neighbour ids rewritten as ranks.
+static eeg_status ensure_pr_rank(eeg_vgraph* vg, cudaStream_t st) {
+    Workspace& ws = vg->ws;
+    if (ws.pr_rcol) return EEG_OK;
+    const uint32_t n = vg->n;
+    const uint64_t slots = (uint64_t)vg->rev.P * vg->K;
+    EEG_TRY(vg_alloc(vg, (void**)&ws.pr_rank, sizeof(uint32_t) * std::max<uint32_t>(n, 1) + 2 * RCLS * sizeof(uint32_t)));
+    uint32_t* hist = ws.pr_rank + n;
+    uint32_t* cursor = hist + RCLS;
+    uint32_t* rcol = nullptr;
+    EEG_TRY(vg_alloc(vg, (void**)&rcol, sizeof(uint32_t) * std::max<uint64_t>(slots, 4)));
+    EEG_CUDA(cudaMemsetAsync(hist, 0, RCLS * sizeof(uint32_t), st));
+    const unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, (uint64_t)sm_count(vg->device) * 8));
+    k_rank_hist<<<g, 256, 0, st>>>(n, vg->fwd.deg, hist);
+    k_rank_base<<<1, 32, 0, st>>>(hist, cursor);
+    const unsigned gt = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + RTILE - 1) / RTILE, (uint64_t)sm_count(vg->device) * 8));
+    k_rank_scatter<<<gt, 256, 0, st>>>(n, vg->fwd.deg, hist, cursor, ws.pr_rank);
+    if (slots) {
+        const unsigned gs = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((slots + 255) / 256, (uint64_t)sm_count(vg->device) * 16));
+        k_rank_cols<<<gs, 256, 0, st>>>(slots, vg->rev.vcol, ws.pr_rank, rcol);
+    }
+    EEG_CUDA(cudaGetLastError());
+    ws.pr_rcol = rcol;
+    return EEG_OK;
+}
+
 eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& o, cudaStream_t st,
                         eeg_result* res) {
     if (!vg->has_rev) {
@@ -325,6 +452,7 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
         return EEG_ERR_INVALID;
     }
     EEG_TRY(ensure_pr_ws(vg));
+    EEG_TRY(ensure_pr_rank(vg, st));
     Workspace& ws = vg->ws;
     const float damping = o.pr_damping > 0.f ? o.pr_damping : 0.85f;
     EEG_CUDA(cudaMemsetAsync(ws.pctrl, 0, sizeof(PRCtrl), st));
@@ -333,8 +461,9 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
     a.RP = (uint32_t)vg->rev.P;
     a.rvstart = vg->rev.vstart;
     a.rvowner = vg->rev.vowner;
-    a.rvcol = vg->rev.vcol;
+    a.rvcol = ws.pr_rcol;
     a.outdeg = vg->fwd.deg;
+    a.rank = ws.pr_rank;
     a.x = ws.x;
     a.c0 = ws.contrib[0];
     a.c1 = ws.contrib[1];
@@ -351,9 +480,9 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
     EEG_CUDA(cudaEventRecord(ws.ev[0], st));
     eeg_status s;
     switch (vg->K) {
-        case 4: s = launch_pr<4>(a, vg->device, o.blocks_per_sm, st); break;
-        case 8: s = launch_pr<8>(a, vg->device, o.blocks_per_sm, st); break;
-        case 16: s = launch_pr<16>(a, vg->device, o.blocks_per_sm, st); break;
+        case 4: s = launch_pr<4>(a, vg->device, o.blocks_per_sm, o.pr_hot_limit, st); break;
+        case 8: s = launch_pr<8>(a, vg->device, o.blocks_per_sm, o.pr_hot_limit, st); break;
+        case 16: s = launch_pr<16>(a, vg->device, o.blocks_per_sm, o.pr_hot_limit, st); break;
         default: set_last_error("K must be 4, 8 or 16"); return EEG_ERR_UNSUPPORTED;
     }
     if (s != EEG_OK) return s;

@@ -200,7 +200,10 @@ typedef struct eeg_options {
     uint32_t host_loop;       /* traversals: 1 = one launch per round with a host round trip in between,
                                  as the reference's do { H2D flag; launch; sync; D2H flag } while loop
                                  (src/eegraph.cu:89-211) -- for comparison; 0 = one persistent launch */
-    uint32_t reserved[7];
+    uint32_t pr_hot_limit;    /* PageRank: at most this many of the highest out-degree vertices have their
+                                 contributions staged in shared memory each sweep (0 = as many as fit;
+                                 1 = none) */
+    uint32_t reserved[6];
 } eeg_options;
 
 typedef struct eeg_result {
