@@ -158,13 +158,18 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     uint32_t epoch = 0;
 
     unsigned long long my_parts = 0, my_edges = 0, my_updates = 0;
+    // BFS seeded with the source only: every round's queue holds exactly the vertices at level `it`
+    // (a round sets values to it+1 only, and a vertex leaves INF once, so atomicMin alone makes each claim
+    // unique). Seeding every vertex (ASYNC_PUSH_DD) makes round 0 dense and in place: a vertex reached in
+    // it may push again in the same round, so levels in a queue mix and claims need the stamps.
+    const bool bfs_levels = OP == OP_BFS && !TD && !a.seed_all;
     uint32_t it = a.it_start;
     bool all_done = true;  // false when this launch stops only because of rounds_limit
     if (a.it_start == 0) {
         // ---- round 0 set-up: values, stamps, initial frontier
         for (uint32_t v = gtid; v < a.n; v += gthreads) {
             a.dist[v] = init_value<OP>(v, a.source);
-            if (!TD) a.stamp[v] = 0u;
+            if (!TD && !bfs_levels) a.stamp[v] = 0u;
         }
         if (!TD && !a.seed_all && blockIdx.x == 0) {
             const uint32_t s0 = a.vstart[a.source], s1 = a.vstart[a.source + 1];
@@ -222,21 +227,32 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             uint32_t d = 0;
             bool active = false;
             if (valid) {
-                const uint32_t v = __ldg(&a.vowner[p]);
-                if (!TD) {  // DD: the part is almost surely live -- fetch its row alongside the owner's value
+                if (bfs_levels) {  // no owner or value load: the level is the round number
                     ld_part<K>(a.vcol + (size_t)p * K, col, pol);
-                    if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
-                }
-                // plain (L1-cached) value reads: the grid barrier's acquire makes the previous round's
-                // values visible; a value improved later in this round re-enqueues its vertex anyway
-                d = a.dist[v];
-                active = !unreached<OP>(d);
-                if (TD && active) {
-                    ld_part<K>(a.vcol + (size_t)p * K, col, pol);
-                    if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                    d = it;
+                    active = true;
+                } else {
+                    const uint32_t v = __ldg(&a.vowner[p]);
+                    if (!TD) {  // DD: the part is almost surely live -- fetch its row alongside the owner's value
+                        ld_part<K>(a.vcol + (size_t)p * K, col, pol);
+                        if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                    }
+                    // plain (L1-cached) value reads: the grid barrier's acquire makes the previous round's
+                    // values visible; a value improved later in this round re-enqueues its vertex anyway
+                    d = a.dist[v];
+                    active = !unreached<OP>(d);
+                    if (TD && active) {
+                        ld_part<K>(a.vcol + (size_t)p * K, col, pol);
+                        if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                    }
                 }
                 if (active) ++my_parts;
             }
+            // all K filter reads are issued before the first atomic (the compiler may not move a load of
+            // dist[] across an atomic on dist[]); a stale value only costs an atomic
+            uint32_t cd[K];
+#pragma unroll
+            for (int i = 0; i < K; ++i) cd[i] = (active && col[i] != NO_EDGE) ? a.dist[col[i]] : 0u;
 #pragma unroll
             for (int i = 0; i < K; ++i) {
                 bool claim = false;
@@ -245,11 +261,12 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                     t = col[i];
                     ++my_edges;
                     const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                    if (better<OP>(nd, a.dist[t])) {  // filter; a stale (larger) value only costs an atomic
+                    if (better<OP>(nd, cd[i])) {
                         const uint32_t prev = atomic_improve<OP>(&a.dist[t], nd);
                         if (better<OP>(nd, prev)) {
                             ++my_updates;
                             if (TD) changed = 1u;
+                            else if (bfs_levels) claim = true;  // atomicMin admits one first improvement
                             else claim = __ldcg(&a.stamp[t]) != tag && atomicExch(&a.stamp[t], tag) != tag;
                         }
                     }
