@@ -42,6 +42,7 @@ EXPORTED = [
     "eeg_batch_create", "eeg_batch_set_queries", "eeg_batch_query_offset", "eeg_batch_run", "eeg_batch_rounds",
     "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_batch_query_times",
     "eeg_ppr_create", "eeg_ppr_set_weights", "eeg_ppr_forward", "eeg_ppr_adjoint", "eeg_ppr_destroy",
+    "eeg_batch_set_grid_queries", "eeg_batch_get_config",
 ]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -127,6 +128,8 @@ def _load() -> C.CDLL:
         "eeg_batch_query_times": (C.c_int, [vp, vp]),
         "eeg_batch_autotune": (C.c_int, [vp, vp, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
         "eeg_batch_destroy": (None, [vp]),
+        "eeg_batch_set_grid_queries": (C.c_int, [vp, C.c_uint32]),
+        "eeg_batch_get_config": (C.c_int, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "eeg_autotune_k": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32),
                                      C.POINTER(C.c_float)]),
         "eeg_ppr_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
@@ -428,6 +431,16 @@ class Batch:
         c, ms = C.c_uint32(), C.c_float()
         _check(_lib.eeg_batch_autotune(self._h, C.c_void_p(out_device_ptr), C.byref(c), C.byref(ms)), "batch_autotune")
         return c.value, ms.value
+
+    def set_grid_queries(self, count: int) -> None:
+        """Run the `count` largest queries one after another on the whole grid before the clusters."""
+        _check(_lib.eeg_batch_set_grid_queries(self._h, count), "batch_set_grid_queries")
+
+    def config(self) -> tuple[int, int]:
+        """(cluster size, whole-grid queries) of the current configuration."""
+        c, g = C.c_uint32(), C.c_uint32()
+        _check(_lib.eeg_batch_get_config(self._h, C.byref(c), C.byref(g)), "batch_get_config")
+        return c.value, g.value
 
     def close(self):
         if self._h:

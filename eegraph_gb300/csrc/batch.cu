@@ -3,10 +3,12 @@
 // No counterpart kernel in the reference: there, every query is a separate eegraph_<algo> call with
 // its own host loop (src/main.cu:74-281 runs them one after another).
 //
-// One launch of k_batch runs a device work queue of queries. The grid is made of thread-block
-// clusters; a cluster takes the next query (largest graphs first: the host sorts them), runs the whole
-// traversal with the cluster's CTAs -- rounds separated by the hardware cluster barrier, frontier = a
-// queue of part ids, the warp-aggregated append of the single-query kernel -- and takes the next query.
+// One launch of k_batch runs a device work queue of queries, largest graphs first (the host sorts them).
+// The first `nbig` queries run one after another on the whole grid (rounds separated by the bounded
+// grid barrier); the grid is made of thread-block clusters, and then each cluster takes the next query,
+// runs the whole traversal with its CTAs -- rounds separated by the hardware cluster barrier, frontier =
+// a queue of part ids, the warp-aggregated append of the single-query kernel -- and takes the next one.
+// The autotuner picks the cluster size and nbig.
 // The launch (with the reset of the work counter) is captured once in a CUDA graph and replayed.
 // Queries run the SYNC_PUSH_DD schedule from their source; results equal every variant's.
 #include <cooperative_groups.h>
@@ -54,21 +56,53 @@ struct BArgs {
     uint32_t* stamp;    // per cluster: scap stamps
     BCtrl* ctrl;        // per cluster
     uint64_t qcap, scap;
+    uint32_t nbig;      // queries [0, nbig) of the size order run on the whole grid first
+    uint32_t pad;
+    uint32_t* tq;       // whole-grid queries: 2 * qcap part ids
+    uint32_t* tstamp;   //                     scap stamps
+    BCtrl* tctrl;
+    BarrierWords* bw;   // grid barrier of the whole-grid phase
+    uint64_t timeout_ns;
+    uint32_t* err;      // set when a queue would exceed its capacity (cannot happen; reported)
 };
 
-// one query on the calling cluster; not inlined, so that each (OP, K) body gets its own registers
-template <int OP, int K>
-__device__ __noinline__ uint32_t cluster_query(const BArgs& a, const BGraph& g, const BQuery& q,
-                                                  const cg::cluster_group& cl, uint32_t* qa, uint32_t* qb,
-                                                  uint32_t* stamp, BCtrl* ctrl, uint32_t& tag, uint32_t* wbuf,
-                                                  uint64_t pol) {
-    const uint32_t crank = cl.block_rank(), csize = cl.num_blocks();
+// The CTAs that run one query together: a thread-block cluster (rounds separated by the hardware
+// cluster barrier), or the whole grid (rounds separated by the bounded grid barrier).
+struct ClusterTeam {
+    cg::cluster_group cl;
+    __device__ uint32_t thread_rank() const { return cl.block_rank() * B_TPB + threadIdx.x; }
+    __device__ uint32_t nthreads() const { return cl.num_blocks() * B_TPB; }
+    __device__ bool leader_cta() const { return cl.block_rank() == 0; }
+    __device__ bool sync() {
+        cl.sync();
+        return true;
+    }
+};
+struct GridTeam {
+    BarrierWords* bw;
+    uint32_t* epoch;
+    uint64_t timeout_ns;
+    __device__ uint32_t thread_rank() const { return blockIdx.x * B_TPB + threadIdx.x; }
+    __device__ uint32_t nthreads() const { return gridDim.x * B_TPB; }
+    __device__ bool leader_cta() const { return blockIdx.x == 0; }
+    __device__ bool sync() { return grid_barrier(bw, *epoch, timeout_ns); }
+};
+
+constexpr uint32_t ABORTED = 0xFFFFFFFFu;
+
+// One query (SYNC_PUSH_DD from its source) on `team`; returns its rounds, or ABORTED when a grid barrier
+// gave up. Not inlined, so that each (OP, K, team) body gets its own registers.
+template <int OP, int K, class Team>
+__device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, const BQuery& q, Team team, uint32_t* qa,
+                                           uint32_t* qb, uint32_t* stamp, BCtrl* ctrl, uint32_t& tag, uint32_t* wbuf,
+                                           uint64_t pol) {
+    const uint32_t trank = team.thread_rank(), tsize = team.nthreads();
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t cwarp = crank * (B_TPB / 32) + (threadIdx.x >> 5), cwarps = csize * (B_TPB / 32);
+    const uint32_t twarp = trank >> 5, twarps = tsize >> 5;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     uint32_t* dist = a.out + q.out_off;
-    for (uint32_t v = crank * B_TPB + threadIdx.x; v < g.n; v += csize * B_TPB) dist[v] = trav::init_value<OP>(v, q.source);
-    if (crank == 0) {
+    for (uint32_t v = trank; v < g.n; v += tsize) dist[v] = trav::init_value<OP>(v, q.source);
+    if (team.leader_cta()) {
         const uint32_t s0 = g.vstart[q.source], s1 = g.vstart[q.source + 1];
         for (uint32_t j = threadIdx.x; j < s1 - s0; j += B_TPB) qa[j] = s0 + j;
         if (threadIdx.x == 0) {
@@ -77,18 +111,22 @@ __device__ __noinline__ uint32_t cluster_query(const BArgs& a, const BGraph& g, 
             ctrl->qparts[2] = 0u;
         }
     }
-    cl.sync();
+    if (!team.sync()) return ABORTED;
     uint32_t it = 0;
     for (;; ++it) {
         const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
-        const uint32_t len = *(volatile uint32_t*)&ctrl->qparts[cur];
+        uint32_t len = *(volatile uint32_t*)&ctrl->qparts[cur];
         if (len == 0u || it >= a.max_rounds) break;
-        if (crank == 0 && threadIdx.x == 0) ctrl->qparts[old] = 0u;
+        if (len > g.P) {  // one claim per vertex per round bounds a round by P parts; never read past it
+            if (threadIdx.x == 0) atomicOr(a.err, 1u);
+            len = g.P;
+        }
+        if (team.leader_cta() && threadIdx.x == 0) ctrl->qparts[old] = 0u;
         ++tag;
         const uint32_t* qcur = (it & 1u) ? qb : qa;
         uint32_t* qnext = (it & 1u) ? qa : qb;
         uint32_t wcnt = 0;
-        for (uint32_t wb = cwarp * 32u; wb < len; wb += cwarps * 32u) {
+        for (uint32_t wb = twarp * 32u; wb < len; wb += twarps * 32u) {
             const uint32_t idx = wb + lane;
             const uint32_t p = idx < len ? qcur[idx] : 0xFFFFFFFFu;
             const bool valid = p < g.P;
@@ -96,12 +134,21 @@ __device__ __noinline__ uint32_t cluster_query(const BArgs& a, const BGraph& g, 
             uint32_t d = 0;
             bool active = false;
             if (valid) {
-                const uint32_t v = __ldg(&g.vowner[p]);
                 ld_part<K>(g.vcol + (size_t)p * K, col, pol);
-                if (OP != OP_BFS) ld_part<K>(g.vw + (size_t)p * K, wt, pol);
-                d = __ldcg(&dist[v]);
-                active = !trav::unreached<OP>(d);
+                if (OP == OP_BFS) {  // source-seeded BFS: a round's queue holds the vertices at level `it`
+                    d = it;
+                    active = true;
+                } else {
+                    const uint32_t v = __ldg(&g.vowner[p]);
+                    ld_part<K>(g.vw + (size_t)p * K, wt, pol);
+                    d = __ldcg(&dist[v]);
+                    active = !trav::unreached<OP>(d);
+                }
             }
+            // every filter read of the part before its first atomic
+            uint32_t cd[K];
+#pragma unroll
+            for (int i = 0; i < K; ++i) cd[i] = (valid && col[i] != NO_EDGE) ? __ldcg(&dist[col[i]]) : 0u;
 #pragma unroll
             for (int i = 0; i < K; ++i) {
                 bool claim = false;
@@ -109,17 +156,19 @@ __device__ __noinline__ uint32_t cluster_query(const BArgs& a, const BGraph& g, 
                 if (active && col[i] != NO_EDGE) {
                     t = col[i];
                     const uint32_t nd = trav::relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                    if (trav::better<OP>(nd, __ldcg(&dist[t]))) {
+                    if (trav::better<OP>(nd, cd[i])) {
                         const uint32_t prev = trav::atomic_improve<OP>(&dist[t], nd);
-                        if (trav::better<OP>(nd, prev))
-                            claim = __ldcg(&stamp[t]) != tag && atomicExch(&stamp[t], tag) != tag;
+                        if (trav::better<OP>(nd, prev)) {
+                            if (OP == OP_BFS) claim = true;  // atomicMin admits one first improvement
+                            else claim = __ldcg(&stamp[t]) != tag && atomicExch(&stamp[t], tag) != tag;
+                        }
                     }
                 }
                 const uint32_t mask = __ballot_sync(0xffffffffu, claim);
                 if (mask) {
                     const uint32_t c = __popc(mask);
                     if (wcnt + c > (uint32_t)trav::WCAP) {
-                        trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane);
+                        trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane, g.P);
                         wcnt = 0;
                     }
                     if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
@@ -127,22 +176,38 @@ __device__ __noinline__ uint32_t cluster_query(const BArgs& a, const BGraph& g, 
                 }
             }
         }
-        if (wcnt) trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane);
-        cl.sync();
+        if (wcnt) trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane, g.P);
+        if (!team.sync()) return ABORTED;
     }
+    // every CTA has read the final (empty) queue length before the leader initialises the next query
+    if (!team.sync()) return ABORTED;
     return it;
 }
 
-template <int OP>
-__device__ __forceinline__ uint32_t dispatch_k(const BArgs& a, const BGraph& g, const BQuery& q,
-                                               const cg::cluster_group& cl, uint32_t* qa, uint32_t* qb,
-                                               uint32_t* stamp, BCtrl* ctrl, uint32_t& tag, uint32_t* wbuf,
-                                               uint64_t pol) {
-    switch (g.K) {
-        case 4: return cluster_query<OP, 4>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol);
-        case 16: return cluster_query<OP, 16>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol);
-        default: return cluster_query<OP, 8>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol);
+template <class Team>
+__device__ __forceinline__ uint32_t dispatch(const BArgs& a, const BGraph& g, const BQuery& q, Team team, uint32_t* qa,
+                                             uint32_t* qb, uint32_t* stamp, BCtrl* ctrl, uint32_t& tag, uint32_t* wbuf,
+                                             uint64_t pol) {
+#define EEG_BATCH_K(OPV)                                                                             \
+    switch (g.K) {                                                                                  \
+        case 4: return run_query<OPV, 4, Team>(a, g, q, team, qa, qb, stamp, ctrl, tag, wbuf, pol);  \
+        case 16: return run_query<OPV, 16, Team>(a, g, q, team, qa, qb, stamp, ctrl, tag, wbuf, pol); \
+        default: return run_query<OPV, 8, Team>(a, g, q, team, qa, qb, stamp, ctrl, tag, wbuf, pol);  \
     }
+    switch (q.op) {
+        case OP_BFS: EEG_BATCH_K(OP_BFS)
+        case OP_SSSP: EEG_BATCH_K(OP_SSSP)
+        default: EEG_BATCH_K(OP_SSWP)
+    }
+#undef EEG_BATCH_K
+}
+
+__device__ __forceinline__ void record(const BArgs& a, const BQuery& q, uint32_t rounds, unsigned long long t0,
+                                       unsigned long long who) {
+    a.rounds[q.input_index] = rounds;
+    a.times[3 * (size_t)q.input_index] = t0;
+    a.times[3 * (size_t)q.input_index + 1] = global_timer_ns();
+    a.times[3 * (size_t)q.input_index + 2] = who;
 }
 
 __global__ void __launch_bounds__(B_TPB, 2) k_batch(BArgs a) {
@@ -152,14 +217,34 @@ __global__ void __launch_bounds__(B_TPB, 2) k_batch(BArgs a) {
     const uint32_t csize = cl.num_blocks(), crank = cl.block_rank();
     const uint32_t cid = blockIdx.x / csize;
     uint32_t* wbuf = s_buf[threadIdx.x >> 5];
+    const uint64_t pol = l2_evict_first_policy();
+
+    // phase 1: the largest queries, one after another, each on the whole grid
+    const uint32_t nbig = min(a.nbig, a.nq);
+    if (nbig) {
+        uint32_t epoch = 0;
+        uint32_t ttag = *(volatile uint32_t*)&a.tctrl->tag;
+        GridTeam gt{a.bw, &epoch, a.timeout_ns};
+        for (uint32_t qi = 0; qi < nbig; ++qi) {
+            const BQuery q = a.queries[qi];
+            const BGraph g = a.graphs[q.graph];
+            const unsigned long long t0 = global_timer_ns();
+            const uint32_t rounds = dispatch(a, g, q, gt, a.tq, a.tq + a.qcap, a.tstamp, a.tctrl, ttag, wbuf, pol);
+            if (rounds == ABORTED) break;
+            if (blockIdx.x == 0 && threadIdx.x == 0) record(a, q, rounds, t0, ~0ull);
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.tctrl->tag = ttag;
+    }
+
+    // phase 2: the rest from the work counter, one query per cluster
     uint32_t* qa = a.q0 + (size_t)cid * 2 * a.qcap;
     uint32_t* qb = qa + a.qcap;
     uint32_t* stamp = a.stamp + (size_t)cid * a.scap;
     BCtrl* ctrl = a.ctrl + cid;
-    const uint64_t pol = l2_evict_first_policy();
     uint32_t tag = *(volatile uint32_t*)&ctrl->tag;
+    ClusterTeam ct{cl};
     for (;;) {
-        if (crank == 0 && threadIdx.x == 0) s_qi = atomicAdd(a.next, 1u);
+        if (crank == 0 && threadIdx.x == 0) s_qi = nbig + atomicAdd(a.next, 1u);
         cl.sync();
         const uint32_t qi = *cl.map_shared_rank(&s_qi, 0);
         cl.sync();  // every CTA has read the index before the leader draws the next one
@@ -167,18 +252,8 @@ __global__ void __launch_bounds__(B_TPB, 2) k_batch(BArgs a) {
         const BQuery q = a.queries[qi];
         const BGraph g = a.graphs[q.graph];
         const unsigned long long t0 = global_timer_ns();
-        uint32_t rounds;
-        switch (q.op) {
-            case OP_BFS: rounds = dispatch_k<OP_BFS>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
-            case OP_SSSP: rounds = dispatch_k<OP_SSSP>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
-            default: rounds = dispatch_k<OP_SSWP>(a, g, q, cl, qa, qb, stamp, ctrl, tag, wbuf, pol); break;
-        }
-        if (crank == 0 && threadIdx.x == 0) {
-            a.rounds[q.input_index] = rounds;
-            a.times[3 * (size_t)q.input_index] = t0;
-            a.times[3 * (size_t)q.input_index + 1] = global_timer_ns();
-            a.times[3 * (size_t)q.input_index + 2] = cid;
-        }
+        const uint32_t rounds = dispatch(a, g, q, ct, qa, qb, stamp, ctrl, tag, wbuf, pol);
+        if (crank == 0 && threadIdx.x == 0) record(a, q, rounds, t0, cid);
     }
     if (crank == 0 && threadIdx.x == 0) ctrl->tag = tag;
 }
@@ -205,6 +280,12 @@ struct eeg_batch {
     BCtrl* d_ctrl = nullptr;
     uint64_t qcap = 0, scap = 0;
     uint32_t nclusters = 0, csize = 0, max_rounds = 0;
+    uint32_t nbig = 0;                 // queries run on the whole grid first
+    uint32_t* d_tq = nullptr;          // their queues and stamps
+    uint32_t* d_tstamp = nullptr;
+    BCtrl* d_tctrl = nullptr;
+    BarrierWords* d_bw = nullptr;
+    uint32_t* d_err = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaGraphExec_t exec = nullptr;
@@ -240,6 +321,13 @@ eeg_status launch(eeg_batch* b, uint32_t* out) {
     a.ctrl = b->d_ctrl;
     a.qcap = b->qcap;
     a.scap = b->scap;
+    a.nbig = b->nbig;
+    a.tq = b->d_tq;
+    a.tstamp = b->d_tstamp;
+    a.tctrl = b->d_tctrl;
+    a.bw = b->d_bw;
+    a.timeout_ns = 1000ull * 1000000ull;  // a round of one query takes microseconds
+    a.err = b->d_err;
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(b->nclusters * b->csize);
     cfg.blockDim = dim3(B_TPB);
@@ -252,6 +340,8 @@ eeg_status launch(eeg_batch* b, uint32_t* out) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     EEG_CUDA(cudaMemsetAsync(b->d_next, 0, sizeof(uint32_t), b->st));
+    EEG_CUDA(cudaMemsetAsync(b->d_bw, 0, sizeof(BarrierWords), b->st));
+    EEG_CUDA(cudaMemsetAsync(b->d_err, 0, sizeof(uint32_t), b->st));
     EEG_CUDA(cudaLaunchKernelEx(&cfg, k_batch, a));
     return EEG_OK;
 }
@@ -343,6 +433,13 @@ EEG_API eeg_status eeg_batch_create(eeg_vgraph* const* graphs, uint32_t num_grap
         (e = cudaEventCreate(&b->ev[0])) != cudaSuccess || (e = cudaEventCreate(&b->ev[1])) != cudaSuccess ||
         (e = cudaMalloc((void**)&b->d_graphs, sizeof(BGraph) * num_graphs)) != cudaSuccess ||
         (e = cudaMalloc((void**)&b->d_next, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_tq, sizeof(uint32_t) * 2 * b->qcap)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_tstamp, sizeof(uint32_t) * b->scap)) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_tctrl, sizeof(BCtrl))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_bw, sizeof(BarrierWords))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_err, sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemset(b->d_tstamp, 0, sizeof(uint32_t) * b->scap)) != cudaSuccess ||
+        (e = cudaMemset(b->d_tctrl, 0, sizeof(BCtrl))) != cudaSuccess ||
         (e = cudaMemcpy(b->d_graphs, hg.data(), sizeof(BGraph) * num_graphs, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(cuda_fail(e, "eeg_batch_create", __FILE__, __LINE__));
     *out = b;
@@ -422,6 +519,44 @@ EEG_API eeg_status eeg_batch_run(eeg_batch* b, uint32_t* out, void* stream, floa
     EEG_CUDA(cudaStreamWaitEvent(user, b->ev[1], 0));
     EEG_CUDA(cudaEventSynchronize(b->ev[1]));
     if (ms) EEG_CUDA(cudaEventElapsedTime(ms, b->ev[0], b->ev[1]));
+    uint32_t err = 0;
+    EEG_CUDA(cudaMemcpy(&err, b->d_err, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err) {
+        set_last_error("eeg_batch_run: internal error: a frontier queue exceeded its capacity");
+        return EEG_ERR_CUDA;
+    }
+    if (b->nbig) {
+        BarrierWords bw{};
+        EEG_CUDA(cudaMemcpy(&bw, b->d_bw, sizeof(bw), cudaMemcpyDeviceToHost));
+        if (bw.status == DEV_TIMEOUT) {
+            set_last_error("eeg_batch_run: a grid barrier wait of the whole-grid phase exceeded the timeout");
+            return EEG_ERR_TIMEOUT;
+        }
+    }
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_batch_set_grid_queries(eeg_batch* b, uint32_t count) {
+    if (!b) {
+        set_last_error("eeg_batch_set_grid_queries: null argument");
+        return EEG_ERR_INVALID;
+    }
+    if (b->nbig != count && b->exec) {  // the captured launch holds the old count
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+        b->captured_out = nullptr;
+    }
+    b->nbig = count;
+    return EEG_OK;
+}
+
+EEG_API eeg_status eeg_batch_get_config(const eeg_batch* b, uint32_t* cluster_size, uint32_t* grid_queries) {
+    if (!b) {
+        set_last_error("eeg_batch_get_config: null argument");
+        return EEG_ERR_INVALID;
+    }
+    if (cluster_size) *cluster_size = b->csize;
+    if (grid_queries) *grid_queries = std::min(b->nbig, b->nq);
     return EEG_OK;
 }
 
@@ -449,21 +584,27 @@ EEG_API eeg_status eeg_batch_autotune(eeg_batch* b, uint32_t* out, uint32_t* cho
         return EEG_ERR_INVALID;
     }
     float best = 3.0e38f;
-    uint32_t best_c = 4;
+    uint32_t best_c = 4, best_big = 0;
     for (uint32_t c : {1u, 2u, 4u, 8u}) {
         if (configure(b, c) != EEG_OK) continue;
-        float t = 0.f, sum = 0.f;
-        bool ok = true;
-        for (int rep = 0; rep < 3 && ok; ++rep) {  // first replay warms up; keep the faster of the others
-            ok = eeg_batch_run(b, out, nullptr, &t) == EEG_OK;
-            if (rep > 0) sum = rep == 1 ? t : std::min(sum, t);
-        }
-        if (ok && sum < best) {
-            best = sum;
-            best_c = c;
+        for (uint32_t nb : {0u, 1u, 2u, 4u, 8u, 16u, 32u, 64u}) {
+            if (nb > b->nq) break;
+            eeg_batch_set_grid_queries(b, nb);
+            float t = 0.f, sum = 0.f;
+            bool ok = true;
+            for (int rep = 0; rep < 3 && ok; ++rep) {  // first replay warms up; keep the faster of the others
+                ok = eeg_batch_run(b, out, nullptr, &t) == EEG_OK;
+                if (rep > 0) sum = rep == 1 ? t : std::min(sum, t);
+            }
+            if (ok && sum < best) {
+                best = sum;
+                best_c = c;
+                best_big = nb;
+            }
         }
     }
     EEG_TRY(configure(b, best_c));
+    eeg_batch_set_grid_queries(b, best_big);
     if (chosen_cluster_size) *chosen_cluster_size = best_c;
     if (best_ms) *best_ms = best;
     return EEG_OK;
@@ -478,6 +619,11 @@ EEG_API void eeg_batch_destroy(eeg_batch* b) {
     cudaFree(b->d_next);
     cudaFree(b->d_rounds);
     cudaFree(b->d_times);
+    cudaFree(b->d_tq);
+    cudaFree(b->d_tstamp);
+    cudaFree(b->d_tctrl);
+    cudaFree(b->d_bw);
+    cudaFree(b->d_err);
     if (b->ev[0]) cudaEventDestroy(b->ev[0]);
     if (b->ev[1]) cudaEventDestroy(b->ev[1]);
     if (b->st) cudaStreamDestroy(b->st);

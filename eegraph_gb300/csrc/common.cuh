@@ -19,7 +19,7 @@ constexpr uint32_t NO_EDGE = 0xFFFFFFFFu;  // unused slot of a part (padding up 
 enum Op : int { OP_BFS = 0, OP_SSSP = 1, OP_SSWP = 2, OP_CC = 3 };
 
 // Device status codes written into control blocks.
-enum DevStatus : uint32_t { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_ITER_CAP = 2, DEV_BAD_INPUT = 3 };
+enum DevStatus : uint32_t { DEV_OK = 0, DEV_TIMEOUT = 1, DEV_ITER_CAP = 2, DEV_BAD_INPUT = 3, DEV_OVERFLOW = 4 };
 
 // ------------------------------------------------------------------ host error plumbing
 void set_last_error(const std::string& msg);

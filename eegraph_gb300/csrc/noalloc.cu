@@ -132,5 +132,9 @@ extern "C" EEG_API eeg_status eeg_run_noalloc(eeg_algo algo, eeg_variant variant
         set_last_error("iteration cap reached before the fixed point");
         return EEG_ERR_ITER_CAP;
     }
+    if (words[2] == DEV_OVERFLOW) {
+        set_last_error("internal error: a frontier queue exceeded its capacity");
+        return EEG_ERR_CUDA;
+    }
     return EEG_OK;
 }

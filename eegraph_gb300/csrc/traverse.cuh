@@ -90,9 +90,11 @@ constexpr int WCAP = 256;  // per-warp append buffer (claimed vertices) before a
 // Warp-cooperative append of the warp's claimed vertices to the next queue: one reservation per flush
 // (atomicAdd of the parts total), then every claimed vertex's part ids are written; a vertex with more
 // than 32 parts is written by the whole warp. Called by all 32 lanes with a warp-uniform `cnt`.
+// Entries at or beyond `cap` are not written (each vertex is claimed once per round, so a round never
+// produces more than `cap` = the number of parts; the reader clamps and reports an overflow).
 __device__ __forceinline__ void warp_append(const uint32_t* __restrict__ vstart, uint32_t* parts_ctr,
                                             uint32_t* verts_ctr, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
-                                            uint32_t lane) {
+                                            uint32_t lane, uint32_t cap) {
     __syncwarp();
     uint32_t sum = 0;
     for (uint32_t e = lane; e < cnt; e += 32u) {
@@ -122,7 +124,8 @@ __device__ __forceinline__ void warp_append(const uint32_t* __restrict__ vstart,
             s0 = vstart[t];
             np = vstart[t + 1] - s0;
             if (np <= 32u)
-                for (uint32_t j = 0; j < np; ++j) qnext[pos + j] = s0 + j;
+                for (uint32_t j = 0; j < np; ++j)
+                    if (pos + j < cap) qnext[pos + j] = s0 + j;
         }
         uint32_t big = __ballot_sync(0xffffffffu, np > 32u);
         while (big) {  // hub vertices: the whole warp writes their part ids
@@ -131,7 +134,8 @@ __device__ __forceinline__ void warp_append(const uint32_t* __restrict__ vstart,
             const uint32_t bs0 = __shfl_sync(0xffffffffu, s0, l);
             const uint32_t bnp = __shfl_sync(0xffffffffu, np, l);
             const uint32_t bpos = __shfl_sync(0xffffffffu, pos, l);
-            for (uint32_t j = lane; j < bnp; j += 32u) qnext[bpos + j] = bs0 + j;
+            for (uint32_t j = lane; j < bnp; j += 32u)
+                if (bpos + j < cap) qnext[bpos + j] = bs0 + j;
         }
         pos += np;
     }
@@ -140,7 +144,7 @@ __device__ __forceinline__ void warp_append(const uint32_t* __restrict__ vstart,
 
 __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* buf, uint32_t cnt, uint32_t* qnext,
                                            uint32_t nxt, uint32_t lane) {
-    warp_append(a.vstart, &a.ctrl->qparts[nxt], &a.ctrl->qverts[nxt], buf, cnt, qnext, lane);
+    warp_append(a.vstart, &a.ctrl->qparts[nxt], &a.ctrl->qverts[nxt], buf, cnt, qnext, lane, a.P);
 }
 
 template <int OP, int K, bool TD>
@@ -199,6 +203,11 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         const bool swap = TD && a.partner && (it & 1u);
         if (dense) len = swap ? (a.P + (a.P & 1u)) : a.P;
         else len = ld_relaxed(&ctrl->qparts[cur]);
+        if (!dense && len > a.P) {  // cannot happen (one claim per vertex per round); never read past the queue
+            if (blockIdx.x == 0 && threadIdx.x == 0)
+                atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
+            len = a.P;
+        }
         if (!dense && len == 0u) break;
         if (it >= a.max_iters) {
             if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_ITER_CAP);
@@ -249,10 +258,12 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                 if (active) ++my_parts;
             }
             // all K filter reads are issued before the first atomic (the compiler may not move a load of
-            // dist[] across an atomic on dist[]); a stale value only costs an atomic
+            // dist[] across an atomic on dist[]); a stale value only costs an atomic. Queued parts are
+            // almost always live, so their filter reads do not wait for the owner's value.
             uint32_t cd[K];
+            const bool fetch = dense ? active : valid;
 #pragma unroll
-            for (int i = 0; i < K; ++i) cd[i] = (active && col[i] != NO_EDGE) ? a.dist[col[i]] : 0u;
+            for (int i = 0; i < K; ++i) cd[i] = (fetch && col[i] != NO_EDGE) ? a.dist[col[i]] : 0u;
 #pragma unroll
             for (int i = 0; i < K; ++i) {
                 bool claim = false;
@@ -267,7 +278,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                             ++my_updates;
                             if (TD) changed = 1u;
                             else if (bfs_levels) claim = true;  // atomicMin admits one first improvement
-                            else claim = __ldcg(&a.stamp[t]) != tag && atomicExch(&a.stamp[t], tag) != tag;
+                            else claim = atomicExch(&a.stamp[t], tag) != tag;
                         }
                     }
                 }

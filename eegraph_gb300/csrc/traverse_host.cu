@@ -140,6 +140,10 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
         set_last_error("iteration cap reached before the fixed point");
         return EEG_ERR_ITER_CAP;
     }
+    if (hc.bw.status == DEV_OVERFLOW) {
+        set_last_error("internal error: a frontier queue exceeded its capacity");
+        return EEG_ERR_CUDA;
+    }
     return EEG_OK;
 }
 

@@ -267,9 +267,14 @@ EEG_API eeg_status eeg_batch_run(eeg_batch* b, uint32_t* out, void* stream, floa
 /* Rounds each query took (num_queries entries, query order). */
 EEG_API eeg_status eeg_batch_rounds(const eeg_batch* b, uint32_t* rounds);
 /* Per query (query order) of the last run: device start and end time (ns, global timer) and the
- * index of the cluster that ran it -- 3 values per query. */
+ * index of the cluster that ran it (~0 for a whole-grid query) -- 3 values per query. */
 EEG_API eeg_status eeg_batch_query_times(const eeg_batch* b, unsigned long long* times);
-/* Autotuner: time the batch with 1, 2, 4 and 8 CTAs per query and keep the fastest. */
+/* The first `count` queries in size order (largest graphs first) run one after another on the whole
+ * grid before the rest are spread over the clusters (0 = none; the default). */
+EEG_API eeg_status eeg_batch_set_grid_queries(eeg_batch* b, uint32_t count);
+EEG_API eeg_status eeg_batch_get_config(const eeg_batch* b, uint32_t* cluster_size, uint32_t* grid_queries);
+/* Autotuner: time the batch with 1, 2, 4 and 8 CTAs per query, each with 0, 1, 2, 4 ... 64 whole-grid
+ * queries, and keep the fastest pair (eeg_batch_get_config reports it). */
 EEG_API eeg_status eeg_batch_autotune(eeg_batch* b, uint32_t* out, uint32_t* chosen_cluster_size, float* best_ms);
 EEG_API void eeg_batch_destroy(eeg_batch* b);
 

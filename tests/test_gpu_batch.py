@@ -82,3 +82,36 @@ def test_autotune_k(gpu):
     assert k in (4, 8, 16) and all(v > 0 for v in ms.values())
     k2, _ = E.autotune_k(1 << 14, s, d, w, reps=2)  # cached
     assert k2 == k
+
+
+@pytest.mark.parametrize("grid_queries", [1, 3, 100])
+def test_batch_whole_grid_queries(gpu, grid_queries):
+    """The largest queries run one after another on the whole grid (bounded grid barrier), the rest on
+    clusters; every query still equals a single eeg_run, and the timeline marks the whole-grid ones."""
+    torch = pytest.importorskip("torch")
+    E = gpu
+    gs = _graphs(E, [(15, 16, 9), (12, 8, 10), (9, 32, 11), (14, 4, 12)])
+    queries = [(0, "bfs", 1), (0, "sssp", 2), (1, "sswp", 3), (2, "bfs", 4), (3, "sssp", 0), (1, "bfs", 0),
+               (3, "sswp", 5)]
+    with E.Batch([g[4] for g in gs]) as b:
+        words = b.set_queries(queries, cluster_size=2)
+        b.set_grid_queries(grid_queries)
+        assert b.config() == (2, min(grid_queries, len(queries)))
+        out = torch.zeros(words, dtype=torch.int32, device="cuda")
+        offs = b.offsets()
+        for _ in range(2):
+            b.run(out.data_ptr())
+            host = out.cpu().numpy().view(np.uint32)
+            for qi, (gi, algo, src) in enumerate(queries):
+                n = gs[gi][0]
+                want, _ = gs[gi][4].run(algo, "sync_push_dd", src)
+                assert np.array_equal(host[offs[qi]:offs[qi] + n], want), (qi, algo)
+        t = b.query_times()
+        whole = t[:, 2] == np.uint64(2**64 - 1)
+        assert int(whole.sum()) == min(grid_queries, len(queries))
+        assert (t[:, 1] >= t[:, 0]).all()
+        # the whole-grid queries are the largest graphs (graph 0 first)
+        sizes = np.array([gs[gi][4].info()["num_parts"] for gi, _, _ in queries])
+        assert sizes[whole].min() >= sizes[~whole].max() if (~whole).any() else True
+    for g in gs:
+        g[4].close()
