@@ -281,9 +281,13 @@ def bench_gpu(args) -> None:
                            "algorithmic_GB": round(by / 1e9, 4),
                            "achieved_GBs": round(by / (ms * 1e-3) / 1e9, 1),
                            "roofline_frac": round(by / (ms * 1e-3) / 1e9 / peak, 4)}
+    kern_names = {"bfs": "k_traverse<OP_BFS>", "sssp": "k_traverse<OP_SSSP>", "sswp": "k_traverse<OP_SSWP>",
+                  "cc": "k_traverse<OP_CC>", "pr": "k_pagerank"}
+    for a in algo_summary:  # measured DRAM bytes per launch (profiles/traffic.json), where captured
+        tr = load_traffic(kern_names[a], f"s{scale}_k{args.pr_k if a == 'pr' else args.k}")
+        algo_summary[a]["dram_GB_per_launch"] = round(tr / 1e9, 3) if tr else None
     dom = max(algo_summary, key=lambda a: algo_summary[a]["kernel_ms"])
-    kern_name = {"bfs": "k_traverse<OP_BFS>", "sssp": "k_traverse<OP_SSSP>", "sswp": "k_traverse<OP_SSWP>",
-                 "cc": "k_traverse<OP_CC>", "pr": "k_pagerank"}[dom]
+    kern_name = kern_names[dom]
     wl = workload_name(scale, args.k, args.pr_k)
     ach = algo_summary[dom]["achieved_GBs"]
     line = {
