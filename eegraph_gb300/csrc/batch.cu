@@ -72,6 +72,8 @@ struct ClusterTeam {
     cg::cluster_group cl;
     __device__ uint32_t thread_rank() const { return cl.block_rank() * B_TPB + threadIdx.x; }
     __device__ uint32_t nthreads() const { return cl.num_blocks() * B_TPB; }
+    __device__ uint32_t cta_rank() const { return cl.block_rank(); }
+    __device__ uint32_t ncta() const { return cl.num_blocks(); }
     __device__ bool leader_cta() const { return cl.block_rank() == 0; }
     __device__ bool sync() {
         cl.sync();
@@ -84,6 +86,8 @@ struct GridTeam {
     uint64_t timeout_ns;
     __device__ uint32_t thread_rank() const { return blockIdx.x * B_TPB + threadIdx.x; }
     __device__ uint32_t nthreads() const { return gridDim.x * B_TPB; }
+    __device__ uint32_t cta_rank() const { return blockIdx.x; }
+    __device__ uint32_t ncta() const { return gridDim.x; }
     __device__ bool leader_cta() const { return blockIdx.x == 0; }
     __device__ bool sync() { return grid_barrier(bw, *epoch, timeout_ns); }
 };
@@ -98,7 +102,9 @@ __device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, cons
                                            uint64_t pol) {
     const uint32_t trank = team.thread_rank(), tsize = team.nthreads();
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t twarp = trank >> 5, twarps = tsize >> 5;
+    const uint32_t crank = team.cta_rank(), ncta = team.ncta();
+    __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;  // ordered before use by the team barrier below
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     uint32_t* dist = a.out + q.out_off;
     for (uint32_t v = trank; v < g.n; v += tsize) dist[v] = trav::init_value<OP>(v, q.source);
@@ -126,8 +132,17 @@ __device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, cons
         const uint32_t* qcur = (it & 1u) ? qb : qa;
         uint32_t* qnext = (it & 1u) ? qa : qb;
         uint32_t wcnt = 0;
-        for (uint32_t wb = twarp * 32u; wb < len; wb += twarps * 32u) {
-            const uint32_t idx = wb + lane;
+        // this CTA's strided share of the round's 32-entry chunks, drawn by its warps from a shared
+        // counter; the other counter is reset for the next round (ordered by the team barrier)
+        if (threadIdx.x == 0) s_next[(it + 1u) & 1u] = 0u;
+        const uint32_t nch = (len + 31u) / 32u;
+        const uint32_t my_chunks = nch > crank ? (nch - crank + ncta - 1u) / ncta : 0u;
+        for (;;) {
+            uint32_t ci = 0;
+            if (lane == 0) ci = atomicAdd(&s_next[it & 1u], 1u);
+            ci = __shfl_sync(0xffffffffu, ci, 0);
+            if (ci >= my_chunks) break;
+            const uint32_t idx = (crank + ci * ncta) * 32u + lane;
             const uint32_t p = idx < len ? qcur[idx] : 0xFFFFFFFFu;
             const bool valid = p < g.P;
             uint32_t col[K], wt[K];

@@ -99,12 +99,12 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
     __shared__ double s_red[2][PR_TPB / 32];
     __shared__ unsigned long long s_zero;
     __shared__ uint2 s_span[PR_TPB / 32][XCAP];
+    __shared__ uint32_t s_next;  // next of this CTA's chunks to hand out in the current sweep
     uint2* xbuf = s_span[threadIdx.x >> 5];
     PRCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * PR_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * PR_TPB;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t gwarp = gtid >> 5, nwarps = gthreads >> 5;
     const uint32_t nchunks = (a.RP + 31u) / 32u;
     const uint64_t pol = l2_evict_first_policy();
     uint32_t epoch = 0;
@@ -159,17 +159,28 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
             {
                 const float4* src4 = reinterpret_cast<const float4*>(ccur);
                 for (uint32_t i = threadIdx.x; i < a.hot / 4u; i += PR_TPB) s_hot4[i] = src4[i];
+                if (threadIdx.x == 0) s_next = 0u;
                 __syncthreads();
             }
 
-            for (uint32_t base = gwarp; base < nchunks; base += nwarps * PR_U) {
+            // This CTA's share of the sweep is the strided chunk set blockIdx.x + i * gridDim.x (a mix of
+            // hub and leaf regions, so CTAs get similar work); its warps draw from it through a shared
+            // counter, so a warp never idles while another warp of the CTA still has chunks queued.
+            const uint32_t my_chunks =
+                nchunks > blockIdx.x ? (nchunks - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u;
+            for (;;) {
+                uint32_t i0 = 0;
+                if (lane == 0) i0 = atomicAdd(&s_next, (uint32_t)PR_U);
+                i0 = __shfl_sync(0xffffffffu, i0, 0);
+                if (i0 >= my_chunks) break;
                 uint32_t v[PR_U], col[PR_U][K], vb[PR_U];
                 bool valid[PR_U];
 #pragma unroll
                 for (int u = 0; u < PR_U; ++u) {
-                    const uint32_t ch = base + (uint32_t)u * nwarps;
+                    const uint32_t ci = i0 + (uint32_t)u;
+                    const uint32_t ch = blockIdx.x + ci * gridDim.x;
                     const uint32_t p = ch * 32u + lane;
-                    valid[u] = ch < nchunks && p < a.RP;
+                    valid[u] = ci < my_chunks && p < a.RP;
                     v[u] = vb[u] = 0xFFFFFFFFu;
                     if (valid[u]) {
                         v[u] = __ldg(&a.rvowner[p]);

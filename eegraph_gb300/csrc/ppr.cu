@@ -207,6 +207,17 @@ __device__ __forceinline__ bool arrive_last(uint32_t* ctr, uint32_t target, uint
     return last != 0;
 }
 
+// Next chunk of this CTA's strided share of the chunk list (blockIdx.x + i * gridDim.x: CTAs get
+// similar mixes of hub and leaf chunks), drawn by its warps through a shared counter so that no warp
+// idles while another of the CTA still has chunks queued. NONE when the share is used up. Warp-collective.
+__device__ __forceinline__ uint32_t next_chunk(uint32_t* ctr, uint32_t nchunks, uint32_t lane) {
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(ctr, 1u);
+    i = __shfl_sync(FULL, i, 0);
+    const uint64_t c = blockIdx.x + (uint64_t)i * gridDim.x;
+    return c < nchunks ? (uint32_t)c : NONE;
+}
+
 // Hub chunk delivery, batched rows. `tot` is the chunk's row (same in both halves). Returns true in
 // the warp that completes the hub for this sweep (`mult` = sweeps completed including this one), with
 // the hub's full row in `out` and its vertex in `v`. Warp-collective.
@@ -307,13 +318,16 @@ __device__ __forceinline__ void flush_row(const SolveArgs& a, float4* out, uint3
     }
 }
 
+// 3 CTAs per SM (<= 85 registers, a few spilled): the solve is latency-bound, and 24 warps per SM
+// instead of 16 measured 1.3x faster on R-MAT s20 x 64 columns.
 template <int K>
-__global__ void __launch_bounds__(PPR_TPB, 2) k_ppr_rows(SolveArgs a) {
+__global__ void __launch_bounds__(PPR_TPB, 3) k_ppr_rows(SolveArgs a) {
     constexpr int U = K >= 16 ? 1 : 16 / K;  // parts per step: 8 row gathers in flight per lane
     constexpr int H = K / 2;                 // slots per half-warp per part
     const uint32_t lane = threadIdx.x & 31u, half = lane >> 4, q = lane & 15u;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
+    __syncthreads();
     const uint64_t pol = l2_evict_first_policy();
     const float4* b = reinterpret_cast<const float4*>(a.b);
     uint32_t epoch = 0, s = 0;
@@ -335,7 +349,8 @@ __global__ void __launch_bounds__(PPR_TPB, 2) k_ppr_rows(SolveArgs a) {
         const float4* in = reinterpret_cast<const float4*>((s & 1u) ? a.y1 : a.y0);
         float4* out = reinterpret_cast<float4*>((s & 1u) ? a.y0 : a.y1);
         double dr = 0.0, dn = 0.0;
-        for (uint32_t c = wid; c < a.g.nchunks; c += nw) {
+        if (threadIdx.x == 0) s_next[(s + 1u) & 1u] = 0u;  // next sweep's; ordered by the sweep's grid barrier
+        for (uint32_t c; (c = next_chunk(&s_next[s & 1u], a.g.nchunks, lane)) != NONE;) {
             const Chunk ch = a.g.chunk[c];
             const uint32_t np = ch.p1 - ch.p0;
             const uint32_t own_l = lane < np ? ld_nc(a.g.vowner + ch.p0 + lane) : NONE;
@@ -423,8 +438,9 @@ __global__ void __launch_bounds__(PPR_TPB, 4) k_ppr_scalar(SolveArgs a) {
     constexpr int PPS = 32 / K;                   // parts per 32-slot step
     constexpr int STEPS = (int)PPR_SLOTS / 32;    // steps per chunk
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
+    __syncthreads();
     const float* b = a.b;
     uint32_t epoch = 0, s = 0;
     bool conv = false;
@@ -438,7 +454,8 @@ __global__ void __launch_bounds__(PPR_TPB, 4) k_ppr_scalar(SolveArgs a) {
         const float* in = (s & 1u) ? a.y1 : a.y0;
         float* out = (s & 1u) ? a.y0 : a.y1;
         double dr = 0.0, dn = 0.0;
-        for (uint32_t c = wid; c < a.g.nchunks; c += nw) {
+        if (threadIdx.x == 0) s_next[(s + 1u) & 1u] = 0u;  // next sweep's; ordered by the sweep's grid barrier
+        for (uint32_t c; (c = next_chunk(&s_next[s & 1u], a.g.nchunks, lane)) != NONE;) {
             const Chunk ch = a.g.chunk[c];
             const uint32_t np = ch.p1 - ch.p0;
             const uint32_t nsl = np * K;
@@ -522,15 +539,16 @@ __global__ void __launch_bounds__(PPR_TPB, 2) k_ppr_grad_rows(GradArgs a) {
     constexpr int U = K >= 16 ? 1 : 16 / K;
     constexpr int H = K / 2;
     const uint32_t lane = threadIdx.x & 31u, half = lane >> 4, q = lane & 15u;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
+    __syncthreads();
     const uint64_t pol = l2_evict_first_policy();
     const float4* X = reinterpret_cast<const float4*>(a.X);
     const float4* L = reinterpret_cast<const float4*>(a.L);
     const uint32_t ri = red_index<H>(q);
     const uint32_t jme = 2u * ri + half;                       // slot this lane reports after the reduction
     const bool writer = (q & (uint32_t)(16 / H - 1)) == 0u;    // one lane per reduced value
-    for (uint32_t c = wid; c < a.g.nchunks; c += nw) {
+    for (uint32_t c; (c = next_chunk(&s_next[0], a.g.nchunks, lane)) != NONE;) {
         const Chunk ch = a.g.chunk[c];
         const uint32_t np = ch.p1 - ch.p0;
         const uint32_t own_l = lane < np ? ld_nc(a.g.vowner + ch.p0 + lane) : NONE;
@@ -607,9 +625,10 @@ __global__ void __launch_bounds__(PPR_TPB, 4) k_ppr_grad_scalar(GradArgs a) {
     constexpr int PPS = 32 / K;
     constexpr int STEPS = (int)PPR_SLOTS / 32;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t c = wid; c < a.g.nchunks; c += nw) {
+    __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
+    __syncthreads();
+    for (uint32_t c; (c = next_chunk(&s_next[0], a.g.nchunks, lane)) != NONE;) {
         const Chunk ch = a.g.chunk[c];
         const uint32_t np = ch.p1 - ch.p0;
         const uint32_t nsl = np * K;

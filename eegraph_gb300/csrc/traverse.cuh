@@ -150,12 +150,12 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
 template <int OP, int K, bool TD>
 __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
+    __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
 
     TravCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * T_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * T_TPB;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t gwarp = gtid >> 5, nwarps = gthreads >> 5;
     const uint32_t lanemask_lt = (1u << lane) - 1u;
     uint32_t* wbuf = s_buf[TD ? 0 : threadIdx.x >> 5];
     const uint64_t pol = l2_evict_first_policy();
@@ -169,6 +169,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     const bool bfs_levels = OP == OP_BFS && !TD && !a.seed_all;
     uint32_t it = a.it_start;
     bool all_done = true;  // false when this launch stops only because of rounds_limit
+    if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
+    __syncthreads();
     if (a.it_start == 0) {
         // ---- round 0 set-up: values, stamps, initial frontier
         for (uint32_t v = gtid; v < a.n; v += gthreads) {
@@ -223,9 +225,19 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         const uint32_t tag = it + 1u;
         uint32_t changed = 0;
         uint32_t wcnt = 0;  // warp-uniform fill of wbuf
+        // This CTA's share of the round is the strided set of 32-entry chunks blockIdx.x + i * gridDim.x;
+        // its warps draw from it through a shared counter (this round's; the other one is reset for the
+        // next round, whose start is ordered by the grid barrier).
+        if (threadIdx.x == 0) s_next[(it + 1u) & 1u] = 0u;
+        const uint32_t nch = (len + 31u) / 32u;
+        const uint32_t my_chunks = nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u;
 
-        for (uint32_t wb = gwarp * 32u; wb < len; wb += nwarps * 32u) {
-            const uint32_t idx = wb + lane;
+        for (;;) {
+            uint32_t ci = 0;
+            if (lane == 0) ci = atomicAdd(&s_next[it & 1u], 1u);
+            ci = __shfl_sync(0xffffffffu, ci, 0);
+            if (ci >= my_chunks) break;
+            const uint32_t idx = (blockIdx.x + ci * gridDim.x) * 32u + lane;
             uint32_t p = 0xFFFFFFFFu;
             if (idx < len) {
                 p = dense ? idx : qcur[idx];
