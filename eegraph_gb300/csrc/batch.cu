@@ -137,13 +137,21 @@ __device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, cons
         if (threadIdx.x == 0) s_next[(it + 1u) & 1u] = 0u;
         const uint32_t nch = (len + 31u) / 32u;
         const uint32_t my_chunks = nch > crank ? (nch - crank + ncta - 1u) / ncta : 0u;
-        for (;;) {
+        // pipelined by one chunk: the next chunk's queue entries load while this one is expanded
+        auto draw = [&](uint32_t& pn) -> uint32_t {
             uint32_t ci = 0;
             if (lane == 0) ci = atomicAdd(&s_next[it & 1u], 1u);
             ci = __shfl_sync(0xffffffffu, ci, 0);
-            if (ci >= my_chunks) break;
             const uint32_t idx = (crank + ci * ncta) * 32u + lane;
-            const uint32_t p = idx < len ? qcur[idx] : 0xFFFFFFFFu;
+            pn = (ci < my_chunks && idx < len) ? qcur[idx] : 0xFFFFFFFFu;
+            return ci;
+        };
+        uint32_t p_next;
+        uint32_t ci_next = draw(p_next);
+        for (;;) {
+            if (ci_next >= my_chunks) break;
+            const uint32_t p = p_next;
+            ci_next = draw(p_next);
             const bool valid = p < g.P;
             uint32_t col[K], wt[K];
             uint32_t d = 0;

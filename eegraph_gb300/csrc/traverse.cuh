@@ -232,17 +232,28 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         const uint32_t nch = (len + 31u) / 32u;
         const uint32_t my_chunks = nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u;
 
-        for (;;) {
+        // Software-pipelined by one chunk: the next chunk is drawn and its queue entries are loaded
+        // before the current chunk is expanded, so the queue load is off each part's dependent chain.
+        auto draw = [&](uint32_t& pn) -> uint32_t {
             uint32_t ci = 0;
             if (lane == 0) ci = atomicAdd(&s_next[it & 1u], 1u);
             ci = __shfl_sync(0xffffffffu, ci, 0);
-            if (ci >= my_chunks) break;
-            const uint32_t idx = (blockIdx.x + ci * gridDim.x) * 32u + lane;
-            uint32_t p = 0xFFFFFFFFu;
-            if (idx < len) {
-                p = dense ? idx : qcur[idx];
-                if (swap) p ^= 1u;
+            pn = 0xFFFFFFFFu;
+            if (ci < my_chunks) {
+                const uint32_t idx = (blockIdx.x + ci * gridDim.x) * 32u + lane;
+                if (idx < len) {
+                    pn = dense ? idx : qcur[idx];
+                    if (swap) pn ^= 1u;
+                }
             }
+            return ci;
+        };
+        uint32_t p_next;
+        uint32_t ci_next = draw(p_next);
+        for (;;) {
+            if (ci_next >= my_chunks) break;
+            const uint32_t p = p_next;
+            ci_next = draw(p_next);
             const bool valid = p < a.P;
             uint32_t col[K], wt[K];
             uint32_t d = 0;
