@@ -570,7 +570,8 @@ def bench_grid(args) -> None:
     """High-diameter road-like graph: 4096 x 4096 grid, 4-neighbour undirected, 10 % of edges deleted,
     0.1 % long-range shortcuts, weights U[1,1000], seed 7. BFS/SSSP/SSWP sync_push_dd from vertex 0, one
     persistent launch each, against the same kernels run one launch per round with a host round trip
-    in between (the reference's loop shape, src/eegraph.cu:89-211)."""
+    in between (the reference's loop shape, src/eegraph.cu:89-211). SSSP and SSWP run bucketed rounds
+    (--grid-delta-sssp / --grid-delta-sswp; 0 = plain rounds), whose plain-round time is reported too."""
     import torch
 
     import eegraph_gb300 as E
@@ -588,19 +589,27 @@ def bench_grid(args) -> None:
     peak, peak_kind = load_peaks()
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     per = {}
+    deltas = {"bfs": 0, "sssp": args.grid_delta_sssp, "sswp": args.grid_delta_sswp}
     with E.VirtualGraph.build(n, s, d, w, K=args.k, stream=stream) as vg, ClockSampler(local) as clk:
         for algo, variant in plan:
+            dl = deltas[algo]
             for _ in range(args.warmup):
-                vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream)
-            pers = [vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream)[1] for _ in range(args.steps)]
-            hl = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, host_loop=True)[1]
+                vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, delta=dl)
+            pers = [vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, delta=dl)[1]
+                    for _ in range(args.steps)]
+            hl = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, host_loop=True, delta=dl)[1]
             ms = statistics.median(r["kernel_ms"] for r in pers)
             r0 = pers[0]
-            per[algo] = {"kernel_ms": round(ms, 3), "rounds": r0["iterations"],
+            per[algo] = {"kernel_ms": round(ms, 3), "rounds": r0["iterations"], "delta": dl,
                          "gteps": round(r0["reached_edges"] / (ms * 1e-3) / 1e9, 3),
                          "roofline_frac": round(r0["algorithmic_bytes"] / (ms * 1e-3) / 1e9 / peak, 4),
+                         "edges_scanned_per_reached_edge": round(r0["edges_scanned"] / max(r0["reached_edges"], 1), 2),
                          "host_loop_ms": round(hl["kernel_ms"], 3),
                          "speedup_vs_host_loop": round(hl["kernel_ms"] / ms, 2)}
+            if dl:
+                plain = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream)[1]
+                per[algo]["plain_rounds_ms"] = round(plain["kernel_ms"], 3)
+                per[algo]["plain_rounds"] = plain["iterations"]
     tot_ms = sum(v["kernel_ms"] for v in per.values())
     tot_e = sum(float(r) for r in [per[a]["gteps"] * per[a]["kernel_ms"] * 1e6 for a in per])
     line = {"metric": "GTEPS (BFS+SSSP+SSWP reached edges / device time) on the 4096^2 road-like grid",
@@ -608,7 +617,8 @@ def bench_grid(args) -> None:
             "warmup": args.warmup, "ms_per_step": round(tot_ms, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded grid, generated in-process)",
             "config": {"workload": f"grid {side}x{side}, 10% edges deleted, 0.1% shortcuts, w~U[1,1000], seed 7, "
-                                   f"source 0, K={args.k}", "vertices": n, "arcs": int(s.size)},
+                                   f"source 0, K={args.k}, bucket widths SSSP {deltas['sssp']} SSWP {deltas['sswp']}",
+                       "vertices": n, "arcs": int(s.size)},
             "per_algo": per, "peak": peak, "peak_source": peak_kind, "clocks": clk.summary()}
     print(json.dumps(line))
 
@@ -735,6 +745,8 @@ def main() -> None:
                          "ppr: personalised PageRank forward + adjoint, 64 teleport vectors, batched vs looped")
     ap.add_argument("--batch-graphs", type=int, default=256)
     ap.add_argument("--grid-side", type=int, default=GRID_SIDE)
+    ap.add_argument("--grid-delta-sssp", type=int, default=8000, help="SSSP bucket width on the grid (0 = plain)")
+    ap.add_argument("--grid-delta-sswp", type=int, default=16, help="SSWP bucket width on the grid (0 = plain)")
     args = ap.parse_args()
     global ALGO_PLAN
     ALGO_PLAN = [p for p in ALGO_PLAN if p[0] in args.algos.split(",")]

@@ -69,6 +69,7 @@ static void free_dir(eeg_vgraph* vg, VDir& d) {
 static void free_ws(eeg_vgraph* vg) {
     Workspace& w = vg->ws;
     vg_free(vg, w.dist);
+    vg_free(vg, w.far);
     vg_free(vg, w.q[0]);
     vg_free(vg, w.q[1]);
     vg_free(vg, w.stamp);

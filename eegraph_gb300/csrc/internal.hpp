@@ -40,6 +40,11 @@ struct TravCtrl {
     unsigned long long parts_processed;
     unsigned long long edges_scanned;
     unsigned long long updates;
+    // bucketed SSSP/SSWP rounds
+    uint32_t fcnt[3];   // far-pile lengths (three piles rotate)
+    uint32_t fmin[3];   // smallest key recorded in each pile
+    uint32_t fcsel[2];  // per round parity: the pile receiving far claims
+    uint32_t tsel[2];   // per round parity: the threshold T
 };
 
 // Control block of the PageRank kernels.
@@ -60,6 +65,7 @@ struct Workspace {
     uint32_t* dist = nullptr;     // n
     uint32_t* q[2] = {nullptr, nullptr};  // P each
     uint32_t* stamp = nullptr;    // n
+    uint32_t* far = nullptr;      // 4n: three far piles and the far flags (bucketed rounds)
     uint32_t* activity = nullptr; // device copy of the activity vector
     uint32_t activity_cap = 0;
     TravCtrl* tctrl = nullptr;

@@ -54,7 +54,9 @@ struct TravArgs {
     uint32_t it_start;     // first round of this launch (0: also the set-up phase)
     uint64_t timeout_ns;
     uint32_t rounds_limit; // rounds this launch may run (host-loop mode: 1); 0 = until done
-    uint32_t pad2;
+    uint32_t delta;        // SSSP/SSWP bucket width (bucketed kernels only)
+    uint32_t* fpile;       // 3 x n far piles (bucketed kernels only)
+    uint32_t* fflag;       // n far flags (1 = in a pile)
 };
 
 template <int OP>
@@ -147,7 +149,15 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
     warp_append(a.vstart, &a.ctrl->qparts[nxt], &a.ctrl->qverts[nxt], buf, cnt, qnext, lane, a.P);
 }
 
-template <int OP, int K, bool TD>
+// BK (SSSP/SSWP, SYNC_PUSH_DD, delta > 0): bucketed rounds. A claimed vertex whose key (SSSP: distance,
+// SSWP: INF - width; smaller is closer in both) is not below the threshold T waits in a far pile (one
+// entry per vertex, marked by its flag) instead of entering the next queue. When the queue runs empty,
+// a far round sets T = smallest recorded far key + delta and moves every far vertex below T back.
+// The fixed point is the same; on high-diameter graphs far fewer edges are rescanned. T and the
+// current pile travel in control words keyed by round parity, so every CTA (and every host-loop
+// launch) reads the value the previous round settled; three piles rotate so that a pile's length is
+// reset two far rounds before it is written again.
+template <int OP, int K, bool TD, bool BK = false>
 __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
     __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
@@ -176,6 +186,15 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         for (uint32_t v = gtid; v < a.n; v += gthreads) {
             a.dist[v] = init_value<OP>(v, a.source);
             if (!TD && !bfs_levels) a.stamp[v] = 0u;
+            if (BK) a.fflag[v] = 0u;
+        }
+        if (BK && blockIdx.x == 0 && threadIdx.x == 0) {
+            for (int i = 0; i < 3; ++i) {
+                ctrl->fcnt[i] = 0u;
+                ctrl->fmin[i] = 0xFFFFFFFFu;
+            }
+            ctrl->fcsel[0] = 0u;  // round 0 (the source's parts) sends every claim to pile 0 (T = 0)
+            ctrl->tsel[0] = 0u;
         }
         if (!TD && !a.seed_all && blockIdx.x == 0) {
             const uint32_t s0 = a.vstart[a.source], s1 = a.vstart[a.source + 1];
@@ -195,11 +214,17 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         }
         const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
         const bool dense = TD || (a.seed_all && it == 0);
+        uint32_t fc = 0, T = 0xFFFFFFFFu, fcount = 0;
+        if (BK) {
+            fc = ld_relaxed(&ctrl->fcsel[it & 1u]);
+            T = ld_relaxed(&ctrl->tsel[it & 1u]);
+            fcount = ld_relaxed(&ctrl->fcnt[fc]);
+        }
         if (it > 0) {
             const uint32_t produced = ld_relaxed(&ctrl->qparts[cur]);
             if (a.activity && blockIdx.x == 0 && threadIdx.x == 0 && it - 1 < a.activity_cap)
                 a.activity[it - 1] = TD ? produced : ld_relaxed(&ctrl->qverts[cur]);
-            if (produced == 0u) break;
+            if (produced == 0u && fcount == 0u) break;
         }
         uint32_t len;
         const bool swap = TD && a.partner && (it & 1u);
@@ -210,7 +235,19 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                 atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
             len = a.P;
         }
-        if (!dense && len == 0u) break;
+        bool far_round = false;
+        if (!dense && len == 0u) {
+            if (!BK || fcount == 0u) break;
+            if (fcount > a.n) {  // one entry per flagged vertex; never read past the pile
+                if (blockIdx.x == 0 && threadIdx.x == 0)
+                    atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
+                fcount = a.n;
+            }
+            far_round = true;
+            const uint32_t fm = ld_relaxed(&ctrl->fmin[fc]);
+            T = fm > 0xFFFFFFFFu - a.delta ? 0xFFFFFFFFu : fm + a.delta;
+        }
+        const uint32_t fdst = far_round ? (fc + 1u) % 3u : fc;  // pile receiving this round's far vertices
         if (it >= a.max_iters) {
             if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_ITER_CAP);
             break;
@@ -218,7 +255,25 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctrl->qparts[old] = 0u;
             ctrl->qverts[old] = 0u;
+            if (BK) {  // what the next round reads; the pile two far rounds back is free again
+                ctrl->fcsel[(it + 1u) & 1u] = fdst;
+                ctrl->tsel[(it + 1u) & 1u] = T;
+                if (far_round) {
+                    ctrl->fcnt[(fc + 2u) % 3u] = 0u;
+                    ctrl->fmin[(fc + 2u) % 3u] = 0xFFFFFFFFu;
+                }
+            }
         }
+        const uint32_t* pile_src = BK ? a.fpile + (size_t)fc * a.n : nullptr;
+        uint32_t* pile_dst = BK ? a.fpile + (size_t)fdst * a.n : nullptr;
+        auto to_far = [&](uint32_t t, uint32_t key) {
+            if (atomicExch(&a.fflag[t], 1u) != 1u) {
+                const uint32_t pos = atomicAdd(&ctrl->fcnt[fdst], 1u);
+                if (pos < a.n) pile_dst[pos] = t;
+                else atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
+            }
+            atomicMin(&ctrl->fmin[fdst], key);
+        };
         // no __restrict__/const-qualified read-only path here: each queue is rewritten every other round
         const uint32_t* qcur = (it & 1u) ? a.q1 : a.q0;
         uint32_t* qnext = (it & 1u) ? a.q0 : a.q1;
@@ -229,7 +284,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         // its warps draw from it through a shared counter (this round's; the other one is reset for the
         // next round, whose start is ordered by the grid barrier).
         if (threadIdx.x == 0) s_next[(it + 1u) & 1u] = 0u;
-        const uint32_t nch = (len + 31u) / 32u;
+        const uint32_t items = far_round ? fcount : len;
+        const uint32_t nch = (items + 31u) / 32u;
         const uint32_t my_chunks = nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u;
 
         // Software-pipelined by one chunk: the next chunk is drawn and its queue entries are loaded
@@ -241,8 +297,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             pn = 0xFFFFFFFFu;
             if (ci < my_chunks) {
                 const uint32_t idx = (blockIdx.x + ci * gridDim.x) * 32u + lane;
-                if (idx < len) {
-                    pn = dense ? idx : qcur[idx];
+                if (idx < items) {
+                    pn = far_round ? pile_src[idx] : (dense ? idx : qcur[idx]);
                     if (swap) pn ^= 1u;
                 }
             }
@@ -254,6 +310,26 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             if (ci_next >= my_chunks) break;
             const uint32_t p = p_next;
             ci_next = draw(p_next);
+            if (BK && far_round) {  // far round: p is a far vertex; move it back when below T
+                bool move = false;
+                if (p < a.n && atomicExch(&a.fflag[p], 0u) == 1u) {
+                    const uint32_t dv = a.dist[p];
+                    const uint32_t key = OP == OP_SSWP ? INF - dv : dv;
+                    if (key < T) move = true;
+                    else to_far(p, key);
+                }
+                const uint32_t mask = __ballot_sync(0xffffffffu, move);
+                if (mask) {
+                    const uint32_t c = __popc(mask);
+                    if (wcnt + c > (uint32_t)WCAP) {
+                        warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
+                        wcnt = 0;
+                    }
+                    if (move) wbuf[wcnt + __popc(mask & lanemask_lt)] = p;
+                    wcnt += c;
+                }
+                continue;
+            }
             const bool valid = p < a.P;
             uint32_t col[K], wt[K];
             uint32_t d = 0;
@@ -302,6 +378,13 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                             if (TD) changed = 1u;
                             else if (bfs_levels) claim = true;  // atomicMin admits one first improvement
                             else claim = atomicExch(&a.stamp[t], tag) != tag;
+                            if (BK && claim) {
+                                const uint32_t key = OP == OP_SSWP ? INF - nd : nd;
+                                if (key >= T) {  // not in this bucket: wait in the far pile
+                                    to_far(t, key);
+                                    claim = false;
+                                }
+                            }
                         }
                     }
                 }
@@ -376,7 +459,8 @@ __global__ void k_reached(const uint32_t* __restrict__ dist, const uint32_t* __r
 
 template <int OP, int K, bool TD>
 eeg_status launch_one(const TravArgs& args, int device, uint32_t blocks_per_sm_req, cudaStream_t st) {
-    auto kern = k_traverse<OP, K, TD>;
+    constexpr bool CAN_BK = !TD && (OP == OP_SSSP || OP == OP_SSWP);
+    auto kern = (CAN_BK && args.delta && !args.seed_all) ? k_traverse<OP, K, TD, CAN_BK> : k_traverse<OP, K, TD, false>;
     int per_sm = 0;
     EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T_TPB, 0));
     if (per_sm <= 0) {

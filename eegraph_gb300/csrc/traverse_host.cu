@@ -66,6 +66,8 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     }
     EEG_TRY(ensure_traversal_ws(vg, activity_host ? activity_cap : 0));
     Workspace& ws = vg->ws;
+    const bool bucketed = o.delta && !td && !seed_all && (op == OP_SSSP || op == OP_SSWP);
+    if (bucketed && !ws.far) EEG_TRY(vg_alloc(vg, (void**)&ws.far, sizeof(uint32_t) * 4 * (size_t)vg->n));
     EEG_CUDA(cudaMemsetAsync(ws.tctrl, 0, sizeof(TravCtrl), st));
 
     TravArgs a{};
@@ -86,6 +88,13 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     a.seed_all = seed_all ? 1u : 0u;
     a.partner = (variant == EEG_SYNC_PUSH_TD) ? 1u : 0u;
     a.max_iters = o.max_iterations ? o.max_iterations : (vg->n > 0xFFFFFFF0u ? 0xFFFFFFFFu : vg->n + 2u);
+    if (bucketed) {
+        // far rounds come on top of the frontier rounds (each moves at least one vertex back)
+        if (!o.max_iterations) a.max_iters = (uint32_t)std::min<uint64_t>(64ull * vg->n + 1024u, 0xFFFFFFF0u);
+        a.delta = o.delta;
+        a.fpile = ws.far;
+        a.fflag = ws.far + 3 * (size_t)vg->n;
+    }
     a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
     a.it_start = 0;
     a.rounds_limit = o.host_loop ? 1u : 0u;

@@ -201,9 +201,12 @@ typedef struct eeg_options {
                                  as the reference's do { H2D flag; launch; sync; D2H flag } while loop
                                  (src/eegraph.cu:89-211) -- for comparison; 0 = one persistent launch */
     uint32_t pr_hot_limit;    /* PageRank: at most this many of the highest out-degree vertices have their
-                                 contributions staged in shared memory each sweep (0 = as many as fit;
-                                 1 = none) */
-    uint32_t reserved[6];
+                                 contributions staged in shared memory each sweep (0 = 32768; 1 = none) */
+    uint32_t delta;           /* SSSP / SSWP with SYNC_PUSH_DD: bucketed rounds of this key width -- a vertex
+                                 whose distance (SSSP) or INF - width (SSWP) is not below the current
+                                 threshold waits until the frontier runs empty (0 = plain rounds). Same
+                                 results; far fewer rescans on high-diameter graphs. */
+    uint32_t reserved[5];
 } eeg_options;
 
 typedef struct eeg_result {
