@@ -100,6 +100,7 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
     __shared__ unsigned long long s_zero;
     __shared__ uint2 s_span[PR_TPB / 32][XCAP];
     __shared__ uint32_t s_next;  // next of this CTA's chunks to hand out in the current sweep
+    __shared__ double s_rn[2];   // the last sweep's residual and norm
     uint2* xbuf = s_span[threadIdx.x >> 5];
     PRCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * PR_TPB + threadIdx.x;
@@ -287,8 +288,15 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
                 atomicAdd(&ctrl->norm[slot], nn);
             }
             if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
-            const double resid = *(volatile double*)&ctrl->resid[slot];
-            const double norm = *(volatile double*)&ctrl->norm[slot] + zero_norm;
+            // one thread per CTA reads the sweep's totals (every warp reading the same two words would
+            // queue at one L2 slice); the CTA takes them from shared memory
+            if (threadIdx.x == 0) {
+                s_rn[0] = *(volatile double*)&ctrl->resid[slot];
+                s_rn[1] = *(volatile double*)&ctrl->norm[slot];
+            }
+            __syncthreads();
+            const double resid = s_rn[0];
+            const double norm = s_rn[1] + zero_norm;
             if (blockIdx.x == 0 && threadIdx.x == 0) {
                 ctrl->last_resid = resid;
                 ctrl->last_norm = norm;

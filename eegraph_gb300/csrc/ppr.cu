@@ -294,7 +294,13 @@ __device__ __forceinline__ int end_sweep(const SolveArgs& a, uint32_t s, double 
         atomicAdd(&ctrl->norm[s % 3], dn);
     }
     if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) return 2;
-    const double resid = __ldcg(&ctrl->resid[s % 3]), norm = __ldcg(&ctrl->norm[s % 3]);
+    __shared__ double s_rn[2];  // one read per CTA instead of one per warp
+    if (threadIdx.x == 0) {
+        s_rn[0] = __ldcg(&ctrl->resid[s % 3]);
+        s_rn[1] = __ldcg(&ctrl->norm[s % 3]);
+    }
+    __syncthreads();
+    const double resid = s_rn[0], norm = s_rn[1];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         // slot (s+2)%3 was last read before barrier s and is next accumulated after barrier s+1
         ctrl->resid[(s + 2) % 3] = 0.0;

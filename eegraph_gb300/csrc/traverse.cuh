@@ -161,6 +161,7 @@ template <int OP, int K, bool TD, bool BK = false>
 __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
     __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
     __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
+    __shared__ uint32_t s_ctl[5];   // this round's control words, read once per CTA
 
     TravCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * T_TPB + threadIdx.x;
@@ -214,14 +215,27 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         }
         const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
         const bool dense = TD || (a.seed_all && it == 0);
+        // one thread per CTA reads the control words the previous round settled (not every warp of the
+        // grid: those same-address reads queue at one L2 slice); the CTA takes them from shared memory
+        if (threadIdx.x == 0) {
+            s_ctl[0] = ld_relaxed(&ctrl->qparts[cur]);
+            if (BK) {
+                const uint32_t f = ld_relaxed(&ctrl->fcsel[it & 1u]);
+                s_ctl[1] = f;
+                s_ctl[2] = ld_relaxed(&ctrl->tsel[it & 1u]);
+                s_ctl[3] = ld_relaxed(&ctrl->fcnt[f]);
+                s_ctl[4] = ld_relaxed(&ctrl->fmin[f]);
+            }
+        }
+        __syncthreads();
         uint32_t fc = 0, T = 0xFFFFFFFFu, fcount = 0;
         if (BK) {
-            fc = ld_relaxed(&ctrl->fcsel[it & 1u]);
-            T = ld_relaxed(&ctrl->tsel[it & 1u]);
-            fcount = ld_relaxed(&ctrl->fcnt[fc]);
+            fc = s_ctl[1];
+            T = s_ctl[2];
+            fcount = s_ctl[3];
         }
         if (it > 0) {
-            const uint32_t produced = ld_relaxed(&ctrl->qparts[cur]);
+            const uint32_t produced = s_ctl[0];
             if (a.activity && blockIdx.x == 0 && threadIdx.x == 0 && it - 1 < a.activity_cap)
                 a.activity[it - 1] = TD ? produced : ld_relaxed(&ctrl->qverts[cur]);
             if (produced == 0u && fcount == 0u) break;
@@ -229,7 +243,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         uint32_t len;
         const bool swap = TD && a.partner && (it & 1u);
         if (dense) len = swap ? (a.P + (a.P & 1u)) : a.P;
-        else len = ld_relaxed(&ctrl->qparts[cur]);
+        else len = s_ctl[0];
         if (!dense && len > a.P) {  // cannot happen (one claim per vertex per round); never read past the queue
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
@@ -244,7 +258,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                 fcount = a.n;
             }
             far_round = true;
-            const uint32_t fm = ld_relaxed(&ctrl->fmin[fc]);
+            const uint32_t fm = s_ctl[4];
             T = fm > 0xFFFFFFFFu - a.delta ? 0xFFFFFFFFu : fm + a.delta;
         }
         const uint32_t fdst = far_round ? (fc + 1u) % 3u : fc;  // pile receiving this round's far vertices
