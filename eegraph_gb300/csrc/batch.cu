@@ -119,9 +119,12 @@ __device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, cons
     }
     if (!team.sync()) return ABORTED;
     uint32_t it = 0;
+    __shared__ uint32_t s_len;  // the round's queue length, read once per CTA
     for (;; ++it) {
         const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
-        uint32_t len = *(volatile uint32_t*)&ctrl->qparts[cur];
+        if (threadIdx.x == 0) s_len = *(volatile uint32_t*)&ctrl->qparts[cur];
+        __syncthreads();
+        uint32_t len = s_len;
         if (len == 0u || it >= a.max_rounds) break;
         if (len > g.P) {  // one claim per vertex per round bounds a round by P parts; never read past it
             if (threadIdx.x == 0) atomicOr(a.err, 1u);
