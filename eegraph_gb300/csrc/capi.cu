@@ -30,6 +30,26 @@ eeg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
     return EEG_ERR_CUDA;
 }
 
+// Graph and workspace arrays come from the device's stream-ordered pool, which keeps freed memory
+// (release threshold raised once per device): a caller that builds and drops graphs repeatedly reuses
+// memory instead of paying cudaMalloc/cudaFree each time. Reuse across streams is made safe by the
+// pool's internal dependencies; handles are destroyed after a device synchronisation (cudaFree's
+// semantics), so no freed array is still in use.
+static void retain_pool_memory(int device) {
+    static std::mutex mu;
+    static bool done[64] = {false};
+    if (device < 0 || device >= 64) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[device]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    (void)cudaGetLastError();
+    done[device] = true;
+}
+
 eeg_status vg_alloc(eeg_vgraph* vg, void** p, size_t bytes) {
     if (bytes == 0) bytes = 4;
     cudaError_t e;
@@ -43,17 +63,22 @@ eeg_status vg_alloc(eeg_vgraph* vg, void** p, size_t bytes) {
             (void)cudaGetLastError();
         }
     } else {
-        e = cudaMalloc(p, bytes);
+        retain_pool_memory(vg->device);
+        e = cudaMallocAsync(p, bytes, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);  // usable from any stream on return
     }
     if (e != cudaSuccess) {
         *p = nullptr;
-        return cuda_fail(e, vg->managed ? "cudaMallocManaged" : "cudaMalloc", __FILE__, __LINE__);
+        return cuda_fail(e, vg->managed ? "cudaMallocManaged" : "cudaMallocAsync", __FILE__, __LINE__);
     }
     return EEG_OK;
 }
 
-void vg_free(eeg_vgraph*, void* p) {
-    if (p) cudaFree(p);
+// Callers synchronise the device first (handle destruction).
+void vg_free(eeg_vgraph* vg, void* p) {
+    if (!p) return;
+    if (vg->managed) cudaFree(p);
+    else cudaFreeAsync(p, 0);
 }
 
 static void free_dir(eeg_vgraph* vg, VDir& d) {
@@ -388,9 +413,11 @@ EEG_API void eeg_vgraph_destroy(eeg_vgraph* vg) {
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(vg->device);
+    cudaDeviceSynchronize();  // no kernel may still use the arrays (cudaFree would have waited too)
     free_dir(vg, vg->fwd);
     free_dir(vg, vg->rev);
     free_ws(vg);
+    cudaStreamSynchronize(0);
     cudaSetDevice(prev);
     delete vg;
 }

@@ -1235,6 +1235,7 @@ EEG_API void eeg_ppr_destroy(eeg_ppr* p) {
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(p->vg->device);
+    cudaDeviceSynchronize();  // no kernel may still use the arrays
     free_pdir(p, p->fwd);
     free_pdir(p, p->rev);
     eeg_vgraph* vg = p->vg;
