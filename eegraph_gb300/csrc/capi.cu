@@ -238,7 +238,10 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         return false;
     };
     const uint32_t *ms = nullptr, *md = nullptr, *mw = nullptr;
-    const bool zero_copy = !on_device && m > 0 && mapped(src, &ms) && mapped(dst, &md) && mapped(w, &mw);
+    // a two-direction build copies the input once (the copy engine moves it as fast as the in-place
+    // reads) instead of reading it over the host link twice
+    const bool zero_copy = !on_device && m > 0 && !(flags & EEG_VG_REVERSE) && mapped(src, &ms) && mapped(dst, &md) &&
+                           mapped(w, &mw);
     cudaEventRecord(e0, st);
     if (zero_copy) {
         ds = ms;
