@@ -28,7 +28,7 @@ VARIANTS = {"async_push_td": ASYNC_PUSH_TD, "async_push_dd": ASYNC_PUSH_DD,
             "sync_push_td": SYNC_PUSH_TD, "sync_push_dd": SYNC_PUSH_DD}
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 DIST_INFINITY = 4294967294
-VG_REVERSE, VG_MANAGED, VG_INPUT_DEVICE, VG_SHIFT_ONE, VG_EDGE_IDS = 1, 2, 4, 8, 16
+VG_REVERSE, VG_MANAGED, VG_INPUT_DEVICE, VG_SHIFT_ONE, VG_EDGE_IDS, VG_SYMMETRIC = 1, 2, 4, 8, 16, 32
 
 # every function the C header declares (checked by the CPU test suite)
 EXPORTED = [
@@ -274,10 +274,12 @@ class VirtualGraph:
 
     @classmethod
     def build(cls, num_nodes: int, src, dst, w=None, K: int = 8, reverse: bool = False, managed: bool = False,
-              stream: int | None = None, shift_one: bool = False, edge_ids: bool = False) -> "VirtualGraph":
-        """Build from host arrays (copied to the device inside the call)."""
+              stream: int | None = None, shift_one: bool = False, edge_ids: bool = False,
+              symmetric: bool = False) -> "VirtualGraph":
+        """Build from host arrays (copied to the device inside the call). symmetric=True declares an
+        undirected edge list (every arc's reverse present with the same weight)."""
         flags = (VG_REVERSE if reverse else 0) | (VG_MANAGED if managed else 0) | (VG_SHIFT_ONE if shift_one else 0)
-        flags |= VG_EDGE_IDS if edge_ids else 0
+        flags |= (VG_EDGE_IDS if edge_ids else 0) | (VG_SYMMETRIC if symmetric else 0)
         h = C.c_void_p()
         src, dst = _u32(src), _u32(dst)
         wi = _u32(w) if w is not None else None

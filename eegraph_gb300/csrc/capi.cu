@@ -263,6 +263,11 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         dw = w ? tmp + 2 * m : nullptr;
     }
     s = build_direction(vg, &vg->fwd, ds, dd, dw, false, st);
+    if (s == EEG_OK && !(flags & EEG_VG_REVERSE) && (flags & EEG_VG_SYMMETRIC)) {
+        vg->rev = vg->fwd;  // undirected: in-edges are the out-edges
+        vg->has_rev = true;
+        vg->rev_alias = true;
+    }
     if (s == EEG_OK && (flags & EEG_VG_REVERSE)) {
         s = build_direction(vg, &vg->rev, ds, dd, nullptr, true, st);
         vg->has_rev = (s == EEG_OK);
@@ -417,8 +422,8 @@ EEG_API void eeg_vgraph_destroy(eeg_vgraph* vg) {
     cudaGetDevice(&prev);
     cudaSetDevice(vg->device);
     cudaDeviceSynchronize();  // no kernel may still use the arrays (cudaFree would have waited too)
+    if (!vg->rev_alias) free_dir(vg, vg->rev);
     free_dir(vg, vg->fwd);
-    free_dir(vg, vg->rev);
     free_ws(vg);
     cudaStreamSynchronize(0);
     cudaSetDevice(prev);

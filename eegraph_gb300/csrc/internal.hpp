@@ -93,6 +93,7 @@ struct eeg_vgraph {
     bool managed = false;
     eeg::VDir fwd, rev;
     bool has_rev = false;
+    bool rev_alias = false;  // EEG_VG_SYMMETRIC: rev shares fwd's arrays
     bool weighted = true;
     uint32_t max_deg = 0, max_deg_vertex = 0;
     uint64_t bytes = 0;

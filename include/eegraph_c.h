@@ -150,8 +150,12 @@ enum {
     EEG_VG_MANAGED = 1u << 1,   /* allocate in managed memory (the --um path) */
     EEG_VG_INPUT_DEVICE = 1u << 2, /* src/dst/weight pointers are device (or managed) pointers */
     EEG_VG_SHIFT_ONE = 1u << 3, /* subtract 1 from every id while building (1-based input) */
-    EEG_VG_EDGE_IDS = 1u << 4   /* keep each slot's input edge index (per-edge results in input order;
+    EEG_VG_EDGE_IDS = 1u << 4,  /* keep each slot's input edge index (per-edge results in input order;
                                    needed by eeg_ppr_create) */
+    EEG_VG_SYMMETRIC = 1u << 5  /* the caller guarantees an undirected edge list (every arc's reverse is
+                                   present with the same weight): the forward graph doubles as the
+                                   transposed one, so PageRank runs without a second build. Ignored with
+                                   REVERSE; not usable by eeg_ppr_create (needs the transposed edge ids). */
 };
 
 typedef struct eeg_vgraph_info {
