@@ -107,6 +107,7 @@ static void free_ws(eeg_vgraph* vg) {
     vg_free(vg, w.arrive);
     vg_free(vg, w.pr_rank);
     vg_free(vg, w.pr_rcol);
+    vg_free(vg, w.pr_info);
     if (w.pctrl) cudaFree(w.pctrl);
     if (w.stats) cudaFree(w.stats);
     if (w.ev[0]) cudaEventDestroy(w.ev[0]);

@@ -76,6 +76,7 @@ struct Workspace {
     uint32_t* arrive = nullptr;   // n (chunks that delivered a partial, per vertex)
     uint32_t* pr_rank = nullptr;  // n (+ class counters): rank of each vertex by out-degree class
     uint32_t* pr_rcol = nullptr;  // transposed graph's neighbour ids as ranks (P_rev * K)
+    uint2* pr_info = nullptr;     // n: (rank, out-degree) of each vertex, one load per finalisation
     PRCtrl* pctrl = nullptr;
     // misc
     unsigned long long* stats = nullptr;  // reached counters

@@ -43,8 +43,7 @@ struct PRArgs {
     const uint32_t* __restrict__ rvstart;
     const uint32_t* __restrict__ rvowner;
     const uint32_t* __restrict__ rvcol;   // transposed graph's neighbours, as ranks (see rank below)
-    const uint32_t* __restrict__ outdeg;
-    const uint32_t* __restrict__ rank;    // position of each vertex in descending out-degree-class order
+    const uint2* __restrict__ info;       // per vertex: (rank in descending out-degree-class order, out-degree)
     uint32_t hot;                         // contributions of ranks < hot are staged in shared memory
     float* x;
     float* c0;
@@ -116,9 +115,10 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
     unsigned long long zero_in = 0;
     for (uint32_t v = gtid; v < a.n; v += gthreads) {
         a.x[v] = a.base;
-        const uint32_t od = a.outdeg[v];
+        const uint2 inf = a.info[v];
+        const uint32_t od = inf.y;
         const float c = od ? a.base / (float)od : 0.f;
-        const uint32_t rk = a.rank[v];
+        const uint32_t rk = inf.x;
         a.c0[rk] = c;
         a.c1[rk] = c;
         a.acc[v] = 0.0;
@@ -153,7 +153,8 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
             double r = 0.0, nrm = 0.0;
             uint32_t nx = 0;  // warp-uniform fill of xbuf
             auto fin = [&](uint32_t vv, double sum) {
-                finalize(a, vv, __ldg(&a.rank[vv]), sum, __ldcg(&a.x[vv]), __ldg(&a.outdeg[vv]), cnext, r, nrm);
+                const uint2 inf = __ldg(&a.info[vv]);
+                finalize(a, vv, inf.x, sum, __ldcg(&a.x[vv]), inf.y, cnext, r, nrm);
             };
             // stage this sweep's hot contributions (the barrier before the sweep ordered every CTA's
             // writes of the previous sweep; ASYNC may see some of this sweep's, which it allows)
@@ -216,9 +217,10 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
                     od[u] = 0u;
                     rk[u] = 0u;
                     if (last[u]) {
-                        rk[u] = __ldg(&a.rank[v[u]]);
+                        const uint2 inf = __ldg(&a.info[v[u]]);
+                        rk[u] = inf.x;
+                        od[u] = inf.y;
                         xo[u] = __ldcg(&a.x[v[u]]);
-                        od[u] = __ldg(&a.outdeg[v[u]]);
                     }
                 }
 #pragma unroll
@@ -408,6 +410,11 @@ __global__ void k_rank_scatter(uint32_t n, const uint32_t* __restrict__ deg, con
         __syncthreads();
     }
 }
+__global__ void k_rank_info(uint32_t n, const uint32_t* __restrict__ rank, const uint32_t* __restrict__ deg,
+                            uint2* __restrict__ info) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        info[v] = make_uint2(rank[v], deg[v]);
+}
 __global__ void k_rank_cols(uint64_t slots, const uint32_t* __restrict__ col, const uint32_t* __restrict__ rank,
                             uint32_t* __restrict__ out) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < slots; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -451,6 +458,8 @@ static eeg_status ensure_pr_rank(eeg_vgraph* vg, cudaStream_t st) {
     k_rank_base<<<1, 32, 0, st>>>(hist, cursor);
     const unsigned gt = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((n + RTILE - 1) / RTILE, (uint64_t)sm_count(vg->device) * 8));
     k_rank_scatter<<<gt, 256, 0, st>>>(n, vg->fwd.deg, hist, cursor, ws.pr_rank);
+    EEG_TRY(vg_alloc(vg, (void**)&ws.pr_info, sizeof(uint2) * std::max<uint32_t>(n, 1)));
+    k_rank_info<<<g, 256, 0, st>>>(n, ws.pr_rank, vg->fwd.deg, ws.pr_info);
     if (slots) {
         const unsigned gs = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((slots + 255) / 256, (uint64_t)sm_count(vg->device) * 16));
         k_rank_cols<<<gs, 256, 0, st>>>(slots, vg->rev.vcol, ws.pr_rank, rcol);
@@ -481,8 +490,7 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
     a.rvstart = vg->rev.vstart;
     a.rvowner = vg->rev.vowner;
     a.rvcol = ws.pr_rcol;
-    a.outdeg = vg->fwd.deg;
-    a.rank = ws.pr_rank;
+    a.info = ws.pr_info;
     a.x = ws.x;
     a.c0 = ws.contrib[0];
     a.c1 = ws.contrib[1];
