@@ -77,6 +77,22 @@ def load_traffic(kernel: str, workload: str):
         return None
 
 
+class EnergyMeter:
+    """GPU energy (joules) over a timed region from the library's NVML session (eeg_energy_*)."""
+
+    def __init__(self, device: int):
+        import eegraph_gb300 as E
+
+        self.session = E.EnergySession(device)
+
+    def summary(self, steps: int, covers: str = "timed steps") -> dict:
+        r = self.session.end()
+        if r is None:
+            return {"unavailable": self.session.reason or "NVML energy counter not available"}
+        return {"joules": round(r["joules"], 3), "joules_per_step": round(r["joules"] / max(steps, 1), 4),
+                "seconds": round(r["seconds"], 4), "avg_watts": round(r["avg_watts"], 1), "covers": covers}
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled during the timed region."""
 
@@ -211,6 +227,7 @@ def bench_gpu(args) -> None:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
+        energy = EnergyMeter(local)
         for i in range(args.steps):
             flush.fill_(float(i))  # L2 flush between timed steps (outside the events)
             starts[i].record()
@@ -224,6 +241,7 @@ def bench_gpu(args) -> None:
                 per_algo[a]["iters"].append(r["iterations"])
                 launches += r["launches"]
         torch.cuda.synchronize()
+        energy_line = energy.summary(args.steps, "timed steps (with their L2 flushes)")
         if world > 1:
             torch.distributed.barrier()
     step_ms = [starts[i].elapsed_time(ends[i]) for i in range(args.steps)]
@@ -315,6 +333,7 @@ def bench_gpu(args) -> None:
                 "d2h_bytes_per_step": d2h, "ms_per_step": round(e2e_total_ms / args.steps, 3)},
         "gpu_launches": launches,
         "clocks": clk.summary(),
+        "energy": energy_line,
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(threads=1, budget_s=args.cpu_budget)
@@ -364,7 +383,9 @@ def bench_batch(args) -> None:
         cluster, _ = b.autotune(out.data_ptr())
         for _ in range(args.warmup):
             b.run(out.data_ptr())
+        energy = EnergyMeter(local)
         batch_ms = [b.run(out.data_ptr()) for _ in range(args.steps)]
+        energy_line = energy.summary(args.steps, "timed batch launches")
         batched = out.cpu().numpy().view(np.uint32).copy()
         offs = b.offsets()
         # plain: the single-query persistent kernel, one call per query, into the same layout
@@ -397,7 +418,7 @@ def bench_batch(args) -> None:
                        "graphs": len(graphs), "queries": len(queries), "edges": total_edges},
             "plain_loop": {"ms_per_step": round(pms, 3), "queries_per_s": round(len(queries) / (pms * 1e-3), 1)},
             "speedup_vs_plain_loop": round(pms / bms, 2), "gteps": round(reached / (bms * 1e-3) / 1e9, 3),
-            "parity_with_plain": same, "clocks": clk.summary()}
+            "parity_with_plain": same, "clocks": clk.summary(), "energy": energy_line}
     print(json.dumps(line))
 
 
@@ -463,7 +484,10 @@ def bench_ppr(args) -> None:
     with E.PPR(vg, C) as pb, ClockSampler(local) as clk:
         pb.set_weights(w)
         step_ms, fwd, adj = [], [], []
+        energy = None
         for i in range(args.warmup + args.steps):
+            if i == args.warmup:
+                energy = EnergyMeter(local)
             flush.zero_()
             torch.cuda.synchronize()
             ev0.record()
@@ -475,6 +499,7 @@ def bench_ppr(args) -> None:
                 step_ms.append(ev0.elapsed_time(ev1))
                 fwd.append(rf)
                 adj.append(ra)
+        energy_line = energy.summary(args.steps, "timed steps (with their L2 flushes)")
         Xb, dwb, dTb = X.cpu().numpy(), dw.cpu().numpy(), dT.cpu().numpy()
         duality = abs(float((Gt.double() * X.double()).sum()) - float((Tt.double() * dT.double()).sum()))
         duality /= float((Gt.double() * X.double()).abs().sum())
@@ -551,6 +576,7 @@ def bench_ppr(args) -> None:
                 "ms_per_step": round(statistics.median(e2e_ms), 3) if e2e_ms else None},
         "gpu_launches": 5,
         "clocks": clk.summary(),
+        "energy": energy_line,
     }
     if not args.no_cpu_baseline:
         cb = ppr_cpu_baseline(args.cpu_budget)
@@ -590,13 +616,23 @@ def bench_grid(args) -> None:
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     per = {}
     deltas = {"bfs": 0, "sssp": args.grid_delta_sssp, "sswp": args.grid_delta_sswp}
+    joules = 0.0
+    energy_ok = True
     with E.VirtualGraph.build(n, s, d, w, K=args.k, stream=stream) as vg, ClockSampler(local) as clk:
         for algo, variant in plan:
             dl = deltas[algo]
             for _ in range(args.warmup):
                 vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, delta=dl)
+            torch.cuda.synchronize()
+            energy = EnergyMeter(local)
             pers = [vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, delta=dl)[1]
                     for _ in range(args.steps)]
+            torch.cuda.synchronize()
+            en = energy.summary(args.steps)
+            if "joules" in en:
+                joules += en["joules"]
+            else:
+                energy_ok = False
             hl = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, host_loop=True, delta=dl)[1]
             ms = statistics.median(r["kernel_ms"] for r in pers)
             r0 = pers[0]
@@ -619,7 +655,10 @@ def bench_grid(args) -> None:
             "config": {"workload": f"grid {side}x{side}, 10% edges deleted, 0.1% shortcuts, w~U[1,1000], seed 7, "
                                    f"source 0, K={args.k}, bucket widths SSSP {deltas['sssp']} SSWP {deltas['sswp']}",
                        "vertices": n, "arcs": int(s.size)},
-            "per_algo": per, "peak": peak, "peak_source": peak_kind, "clocks": clk.summary()}
+            "per_algo": per, "peak": peak, "peak_source": peak_kind, "clocks": clk.summary(),
+            "energy": ({"joules": round(joules, 3), "joules_per_step": round(joules / args.steps, 4),
+                        "covers": "timed persistent runs of the three algorithms"} if energy_ok
+                       else {"unavailable": "NVML energy counter not available"})}
     print(json.dumps(line))
 
 

@@ -52,3 +52,16 @@ def test_bad_k_rejected():
 def test_unreadable_graph_reports():
     r = _run("--input", "/nonexistent/graph.el")
     assert "Error reading graph" in r.stdout or "Graph file not read correctly" in r.stdout
+
+
+def test_sweep_command_line():
+    """sweep-main (the reference's src/main.cu measurement sweep): usage, bad options, bad variant."""
+    exe = str(BIN / "sweep-main")
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "--graphs" in r.stdout
+    assert subprocess.run([exe], capture_output=True, text=True, timeout=60).returncode == 2
+    assert subprocess.run([exe, "--graphs", "x.el", "--bogus"], capture_output=True, text=True,
+                          timeout=60).returncode == 2
+    r = subprocess.run([exe, "--graphs", "x.el", "--variants", "sync-push-xx"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 2 and "unknown variant" in r.stderr

@@ -88,3 +88,31 @@ def test_cli_one_based_file_and_activity(tmp_path, gpu):
     n = int(max(s.max(), d.max())) + 1
     got = _read_out(out, np.uint64)
     assert np.array_equal(got, oracle.bfs(n, s, d, 0).astype(np.uint64)[: got.size])
+
+
+def test_sweep_writes_the_reference_layout(tmp_path):
+    """sweep-main runs every (framework, energy, algorithm, trial, variant) and writes the reference's
+    files: <algo>/<bench>[-energy]/[um-]<variant><trial> holding the program's timing lines, plus the
+    energy readings/stats files (or the 'Energy unavailable' line where NVML is missing)."""
+    import eegraph_gb300 as E
+
+    s, d, w = E.gen_rmat(9, 8, seed=51, wmin=1, wmax=63)
+    g = tmp_path / "tiny.wel"
+    _write_wel(g, s, d, w)
+    out = tmp_path / "sweep"
+    r = subprocess.run([str(BIN / "sweep-main"), "--graphs", str(g), "--names", "tiny", "--trials", "2",
+                        "--algos", "bfs,sssp,pr", "--frameworks", "classic,um", "--energy", "both", "--out", str(out)],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    for algo in ("bfs", "sssp", "pr"):
+        for sub in ("tiny", "tiny-energy"):
+            for prefix in ("", "um-"):
+                for v in ("async-push-td", "async-push-dd", "sync-push-td", "sync-push-dd"):
+                    for t in (0, 1):
+                        f = out / algo / sub / f"{prefix}{v}{t}"
+                        text = f.read_text()
+                        assert "Processing finished in" in text, (f, text)
+                        if sub.endswith("energy"):
+                            assert ("Energy consumed" in text) or ("Energy unavailable" in text), text
+                            if "Energy consumed" in text:
+                                assert (out / algo / sub / f"{prefix}{v}-stats{t}").exists()
