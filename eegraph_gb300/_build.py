@@ -80,7 +80,8 @@ def build(verbose: bool = False, jobs: int | None = None, verbose_ptxas: bool = 
     hdrs = _headers()
     units = [(CSRC / s, OBJ / (Path(s).stem + ".o")) for s in CU_SOURCES + CPP_SOURCES]
     fac = [(CSRC / s, OBJ / ("facade_" + Path(s).stem + ".o")) for s in FACADE_SOURCES]
-    cli = [(CSRC / "cli" / "main.cpp", OBJ / "cli_main.o"), (CSRC / "cli" / "sweep.cpp", OBJ / "cli_sweep.o")]
+    cli = [(CSRC / "cli" / "main.cpp", OBJ / "cli_main.o"), (CSRC / "cli" / "sweep.cpp", OBJ / "cli_sweep.o"),
+           (CSRC / "cli" / "graph_info.cpp", OBJ / "cli_graph_info.o")]
     jobs = jobs or max(2, min(16, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_compile, s, o, hdrs, verbose_ptxas) for s, o in units + fac + cli]
@@ -103,7 +104,7 @@ def build(verbose: bool = False, jobs: int | None = None, verbose_ptxas: bool = 
     BIN.mkdir(parents=True, exist_ok=True)
     # the per-algorithm programs (one program; it picks the algorithm from the name it is started
     # under) and the measurement sweep
-    for exe, obj in [(e, cli[0][1]) for e in CLI] + [("sweep-main", cli[1][1])]:
+    for exe, obj in [(e, cli[0][1]) for e in CLI] + [("sweep-main", cli[1][1]), ("graph-info-main", cli[2][1])]:
         target = BIN / exe
         if _stale(target, [obj, fac_lib, lib]):
             _run(["g++", "-o", str(target), str(obj), "-L", str(LIB),

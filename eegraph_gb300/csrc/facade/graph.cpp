@@ -1,6 +1,8 @@
-// graph.cpp -- Graph / UMGraph of the C++ facade (reference src/graph.cpp:1-120, src/um_graph.cu:1-122).
-// Parsing is done by eeg_graph_load (same rules as the reference, multi-threaded); these classes
-// keep the reference's public fields and console output.
+// graph.cpp -- Graph / UMGraph / VertexSubgraph of the C++ facade (reference src/graph.cpp:1-203,
+// src/um_graph.cu:1-122). Parsing is done by eeg_graph_load (same rules as the reference,
+// multi-threaded); these classes keep the reference's public fields and console output.
+#include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
@@ -102,4 +104,60 @@ void UMGraph::ReadGraph() {
     std::cout << "Done reading.\n";
     std::cout << "Number of nodes = " << num_nodes << std::endl;
     std::cout << "Number of edges = " << num_edges << std::endl;
+}
+
+// ------------------------------------------------------------------ VertexSubgraph
+VertexSubgraph::VertexSubgraph(Graph& graph, std::string graphFilePath, bool isWeighted)
+    : Graph(graphFilePath, isWeighted), parentGraph(&graph) {}
+
+VertexSubgraph::~VertexSubgraph() { delete[] selected; }
+
+void VertexSubgraph::MakeSubgraph(float pct_, int sourceNode, time_t seed) {
+    graphLoaded = parentGraph->graphLoaded;
+    pct = pct_;
+    if (!graphLoaded) {
+        std::cout << "Graph has not been loaded" << std::endl;
+        return;
+    }
+    const uint n = parentGraph->num_nodes;
+    num_nodes = n;
+    const double want = std::min(1.0, std::max(0.0, (double)pct)) * n;
+    subgraph_num_nodes = (uint)want;
+    Timer overhead;
+    overhead.Start();
+    delete[] selected;
+    selected = new bool[n ? n : 1]();
+    uint count = 0;
+    if (n > 0 && sourceNode >= 0 && (uint)sourceNode < n) {
+        selected[sourceNode] = true;
+        count = 1;
+    }
+    srand((unsigned)seed);
+    const uint low = n / 5 ? n / 5 : n;  // the first half of the draws come from the lowest fifth of the ids
+    while (count < subgraph_num_nodes) {
+        const uint r = (uint)rand();
+        const uint v = count < subgraph_num_nodes / 2 ? r % low : r % n;
+        if (!selected[v]) {
+            selected[v] = true;
+            ++count;
+        }
+    }
+    edges.clear();
+    weights.clear();
+    hasZeroID = false;
+    for (size_t i = 0; i < parentGraph->edges.size(); ++i) {
+        const Edge e = parentGraph->edges[i];
+        if (e.source < n && e.end < n && selected[e.source] && selected[e.end]) {
+            if (e.source == 0 || e.end == 0) hasZeroID = true;
+            if (isWeighted) weights.push_back(i < parentGraph->weights.size() ? parentGraph->weights[i] : 1u);
+            edges.push_back(e);
+        }
+    }
+    num_edges = (uint)edges.size();
+    const float ms = overhead.Finish();
+    std::cout << "Done generating subgraph.\n";
+    std::cout << "Subgraph generated in " << ms << " (ms)" << std::endl;
+    std::cout << "Subgraph number of nodes = " << subgraph_num_nodes << std::endl;
+    std::cout << "Virtual graph assumed number of nodes = " << num_nodes << std::endl;
+    std::cout << "Subgraph number of edges = " << num_edges << std::endl;
 }

@@ -17,6 +17,7 @@
 #include <sys/time.h>
 
 #include <climits>
+#include <ctime>
 #include <string>
 #include <vector>
 
@@ -88,6 +89,26 @@ class Graph {
     Graph(std::string graphFilePath, bool isWeighted);
     void ReadGraph();
     std::string getFileExtension(std::string fileName);
+};
+
+// Vertex-induced subgraph for experiments (reference include/graph.hpp:52-63, src/graph.cpp:122-203):
+// MakeSubgraph keeps pct of the parent's vertices -- the source, then vertices drawn with the C library's
+// rand() seeded by `seed`, the first half of the draws from the lowest fifth of the ids -- and the edges
+// whose both ends are kept. Ids are not renumbered (num_nodes stays the parent's, as the reference's
+// "Virtual graph assumed number of nodes" line says). The same seed on the same C library gives the same
+// subgraph. Unlike the reference it also works for graphs under five vertices and stops at 100 %.
+class VertexSubgraph : public Graph {
+   public:
+    Graph* parentGraph;
+    float pct = 0.f;
+    bool* selected = nullptr;
+    uint subgraph_num_nodes = 0;  // kept vertices (to pass into VirtualGraph)
+
+    VertexSubgraph(Graph& graph, std::string graphFilePath, bool isWeighted);
+    ~VertexSubgraph();
+    VertexSubgraph(const VertexSubgraph&) = delete;
+    VertexSubgraph& operator=(const VertexSubgraph&) = delete;
+    void MakeSubgraph(float pct, int sourceNode, time_t seed);
 };
 
 // Managed-memory twin: edges/weights live in cudaMallocManaged memory.

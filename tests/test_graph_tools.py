@@ -1,0 +1,93 @@
+"""Experiment tools of the reference on the C++ facade (CPU only): graph-info-main (src/graph_info.cpp)
+and VertexSubgraph::MakeSubgraph (src/graph.cpp:122-203)."""
+import ctypes
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+BIN = ROOT / "eegraph_gb300" / "_bin"
+LIB = ROOT / "eegraph_gb300" / "_lib"
+
+
+def _graph(tmp_path, n=400, m=3000, seed=5):
+    rng = np.random.default_rng(seed)
+    s = rng.integers(0, n, m)
+    d = rng.integers(0, n, m)
+    s[:20] = 0  # a hub at id 0 (the file is 0-based)
+    w = rng.integers(1, 64, m)
+    p = tmp_path / "g.wel"
+    with open(p, "w") as f:
+        f.write("# test graph\n")
+        for a, b, c in zip(s, d, w):
+            f.write(f"{a} {b} {c}\n")
+    return p, s, d, w
+
+
+def test_graph_info_numbers(tmp_path):
+    p, s, d, w = _graph(tmp_path)
+    r = subprocess.run([str(BIN / "graph-info-main"), "--input", str(p)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n = int(max(s.max(), d.max())) + 1
+    deg = np.bincount(s, minlength=n)
+    cut = int(0.2 * n)
+    vals = {line.split(":")[0]: float(line.split(":")[1]) for line in r.stdout.splitlines() if ":" in line
+            and line.split(":")[0] in ("Max degree", "Avg Degree First 20 percent of Vertices",
+                                       "Avg Degree Remaining 80 percent of Vertices")}
+    assert vals["Max degree"] == deg.max()
+    assert abs(vals["Avg Degree First 20 percent of Vertices"] - deg[:cut].mean()) < 1e-3
+    assert abs(vals["Avg Degree Remaining 80 percent of Vertices"] - deg[cut:].mean()) < 1e-3
+
+
+DRIVER = r'''
+#include <iostream>
+#include "eegraph.hpp"
+int main(int argc, char** argv) {
+    Graph g(argv[1], true);
+    g.ReadGraph();
+    VertexSubgraph sub(g, argv[1], true);
+    sub.MakeSubgraph(std::stof(argv[2]), std::stoi(argv[3]), (time_t)std::stol(argv[4]));
+    std::cout << "SEL";
+    for (uint v = 0; v < sub.num_nodes; ++v) if (sub.selected[v]) std::cout << " " << v;
+    std::cout << "\nEDGES " << sub.num_edges << "\n";
+    for (uint e = 0; e < sub.num_edges; ++e)
+        std::cout << sub.edges[e].source << " " << sub.edges[e].end << " " << sub.weights[e] << "\n";
+}
+'''
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a C++ compiler")
+def test_vertex_subgraph_selection_and_induced_edges(tmp_path):
+    p, s, d, w = _graph(tmp_path)
+    src = tmp_path / "drv.cpp"
+    src.write_text(DRIVER)
+    exe = tmp_path / "drv"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-o", str(exe), str(src), "-I", str(ROOT / "include"),
+                    "-L", str(LIB), "-leegraph_facade", "-leegraph", f"-Wl,-rpath,{LIB}", "-pthread"],
+                   check=True, timeout=120)
+    pct, source, seed = 0.3, 7, 12345
+    r = subprocess.run([str(exe), str(p), str(pct), str(source), str(seed)], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.splitlines()
+    sel_line = next(l for l in lines if l.startswith("SEL"))
+    got_sel = set(int(x) for x in sel_line.split()[1:])
+    k = next(i for i, l in enumerate(lines) if l.startswith("EDGES "))
+    got_edges = [tuple(map(int, l.split())) for l in lines[k + 1:k + 1 + int(lines[k].split()[1])]]
+    # the selection restated with the same C library's generator
+    libc = ctypes.CDLL(None)
+    n = int(max(s.max(), d.max())) + 1
+    want_n = int(pct * n)
+    sel = {source}
+    libc.srand(ctypes.c_uint(seed))
+    while len(sel) < want_n:
+        rnd = libc.rand()
+        v = rnd % (n // 5) if len(sel) < want_n // 2 else rnd % n
+        sel.add(v)
+    assert got_sel == sel
+    want_edges = [(a, b, c) for a, b, c in zip(s.tolist(), d.tolist(), w.tolist()) if a in sel and b in sel]
+    assert got_edges == want_edges
+    assert "Subgraph number of edges = %d" % len(want_edges) in r.stdout
