@@ -6,6 +6,7 @@
 #include <cstring>
 #include <iostream>
 #include <stdexcept>
+#include <vector>
 
 #include "eegraph.hpp"
 
@@ -112,6 +113,40 @@ VertexSubgraph::VertexSubgraph(Graph& graph, std::string graphFilePath, bool isW
 
 VertexSubgraph::~VertexSubgraph() { delete[] selected; }
 
+namespace {
+
+// pct of the n vertices: the source, then rand() draws seeded by `seed`, the first half of them from
+// the lowest fifth of the ids. Returns the number kept; `selected` must hold n zeroed flags.
+uint select_vertices(uint n, float pct, int sourceNode, time_t seed, bool* selected) {
+    const uint target = (uint)(std::min(1.0, std::max(0.0, (double)pct)) * n);
+    uint count = 0;
+    if (n > 0 && sourceNode >= 0 && (uint)sourceNode < n) {
+        selected[sourceNode] = true;
+        count = 1;
+    }
+    srand((unsigned)seed);
+    const uint low = n / 5 ? n / 5 : n;
+    while (count < target) {
+        const uint r = (uint)rand();
+        const uint v = count < target / 2 ? r % low : r % n;
+        if (!selected[v]) {
+            selected[v] = true;
+            ++count;
+        }
+    }
+    return target;
+}
+
+void print_subgraph(float ms, uint kept, uint n, uint m) {
+    std::cout << "Done generating subgraph.\n";
+    std::cout << "Subgraph generated in " << ms << " (ms)" << std::endl;
+    std::cout << "Subgraph number of nodes = " << kept << std::endl;
+    std::cout << "Virtual graph assumed number of nodes = " << n << std::endl;
+    std::cout << "Subgraph number of edges = " << m << std::endl;
+}
+
+}  // namespace
+
 void VertexSubgraph::MakeSubgraph(float pct_, int sourceNode, time_t seed) {
     graphLoaded = parentGraph->graphLoaded;
     pct = pct_;
@@ -121,27 +156,11 @@ void VertexSubgraph::MakeSubgraph(float pct_, int sourceNode, time_t seed) {
     }
     const uint n = parentGraph->num_nodes;
     num_nodes = n;
-    const double want = std::min(1.0, std::max(0.0, (double)pct)) * n;
-    subgraph_num_nodes = (uint)want;
     Timer overhead;
     overhead.Start();
     delete[] selected;
     selected = new bool[n ? n : 1]();
-    uint count = 0;
-    if (n > 0 && sourceNode >= 0 && (uint)sourceNode < n) {
-        selected[sourceNode] = true;
-        count = 1;
-    }
-    srand((unsigned)seed);
-    const uint low = n / 5 ? n / 5 : n;  // the first half of the draws come from the lowest fifth of the ids
-    while (count < subgraph_num_nodes) {
-        const uint r = (uint)rand();
-        const uint v = count < subgraph_num_nodes / 2 ? r % low : r % n;
-        if (!selected[v]) {
-            selected[v] = true;
-            ++count;
-        }
-    }
+    subgraph_num_nodes = select_vertices(n, pct, sourceNode, seed, selected);
     edges.clear();
     weights.clear();
     hasZeroID = false;
@@ -154,10 +173,49 @@ void VertexSubgraph::MakeSubgraph(float pct_, int sourceNode, time_t seed) {
         }
     }
     num_edges = (uint)edges.size();
-    const float ms = overhead.Finish();
-    std::cout << "Done generating subgraph.\n";
-    std::cout << "Subgraph generated in " << ms << " (ms)" << std::endl;
-    std::cout << "Subgraph number of nodes = " << subgraph_num_nodes << std::endl;
-    std::cout << "Virtual graph assumed number of nodes = " << num_nodes << std::endl;
-    std::cout << "Subgraph number of edges = " << num_edges << std::endl;
+    print_subgraph(overhead.Finish(), subgraph_num_nodes, num_nodes, num_edges);
+}
+
+// ------------------------------------------------------------------ UMVertexSubgraph
+UMVertexSubgraph::UMVertexSubgraph(UMGraph& graph, std::string graphFilePath, bool isWeighted)
+    : UMGraph(graphFilePath, isWeighted), parentGraph(&graph) {}
+
+UMVertexSubgraph::~UMVertexSubgraph() { delete[] selected; }
+
+void UMVertexSubgraph::MakeSubgraph(float pct_, int sourceNode, time_t seed) {
+    graphLoaded = parentGraph->graphLoaded;
+    pct = pct_;
+    if (!graphLoaded) {
+        std::cout << "Graph has not been loaded" << std::endl;
+        return;
+    }
+    const uint n = parentGraph->num_nodes;
+    num_nodes = n;
+    Timer overhead;
+    overhead.Start();
+    delete[] selected;
+    selected = new bool[n ? n : 1]();
+    subgraph_num_nodes = select_vertices(n, pct, sourceNode, seed, selected);
+    std::vector<Edge> ke;
+    std::vector<uint> kw;
+    hasZeroID = false;
+    for (uint i = 0; i < parentGraph->num_edges; ++i) {
+        const Edge e = parentGraph->edges[i];
+        if (e.source < n && e.end < n && selected[e.source] && selected[e.end]) {
+            if (e.source == 0 || e.end == 0) hasZeroID = true;
+            ke.push_back(e);
+            kw.push_back(parentGraph->weights ? parentGraph->weights[i] : 1u);
+        }
+    }
+    eeg_managed_free(edges);
+    eeg_managed_free(weights);
+    edges = nullptr;
+    weights = nullptr;
+    if (eeg_managed_alloc(sizeof(Edge) * (ke.empty() ? 1 : ke.size()), (void**)&edges) != EEG_OK ||
+        eeg_managed_alloc(sizeof(uint) * (kw.empty() ? 1 : kw.size()), (void**)&weights) != EEG_OK)
+        throw std::runtime_error(std::string("UMVertexSubgraph: ") + eeg_last_error());
+    std::copy(ke.begin(), ke.end(), edges);
+    std::copy(kw.begin(), kw.end(), weights);
+    num_edges = (uint)ke.size();
+    print_subgraph(overhead.Finish(), subgraph_num_nodes, num_nodes, num_edges);
 }

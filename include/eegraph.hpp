@@ -130,6 +130,22 @@ class UMGraph {
     std::string getFileExtension(std::string fileName);
 };
 
+// Managed-memory twin of VertexSubgraph (reference include/um_graph.cuh:52-63, src/um_graph.cu:124-200):
+// the same selection; the kept edges and weights go to cudaMallocManaged arrays.
+class UMVertexSubgraph : public UMGraph {
+   public:
+    UMGraph* parentGraph;
+    float pct = 0.f;
+    bool* selected = nullptr;
+    uint subgraph_num_nodes = 0;
+
+    UMVertexSubgraph(UMGraph& graph, std::string graphFilePath, bool isWeighted);
+    ~UMVertexSubgraph();
+    UMVertexSubgraph(const UMVertexSubgraph&) = delete;
+    UMVertexSubgraph& operator=(const UMVertexSubgraph&) = delete;
+    void MakeSubgraph(float pct, int sourceNode, time_t seed);
+};
+
 // K-bounded virtual graph. The constructor shifts 1-based ids down by one in the Graph it is
 // given and counts degrees, as the reference's does. MakeGraph() builds the lossless virtual graph
 // on the GPU and fills the public host arrays in the reference layout (nodePointer, edgeList =

@@ -116,3 +116,53 @@ def test_sweep_writes_the_reference_layout(tmp_path):
                             assert ("Energy consumed" in text) or ("Energy unavailable" in text), text
                             if "Energy consumed" in text:
                                 assert (out / algo / sub / f"{prefix}{v}-stats{t}").exists()
+
+
+UM_SUB_DRIVER = r'''
+#include <iostream>
+#include "eegraph.hpp"
+int main(int argc, char** argv) {
+    Graph g(argv[1], true);
+    g.ReadGraph();
+    VertexSubgraph a(g, argv[1], true);
+    a.MakeSubgraph(0.4f, 3, (time_t)99);
+    UMGraph ug(argv[1], true);
+    ug.ReadGraph();
+    UMVertexSubgraph b(ug, argv[1], true);
+    b.MakeSubgraph(0.4f, 3, (time_t)99);
+    bool same = a.num_edges == b.num_edges && a.subgraph_num_nodes == b.subgraph_num_nodes;
+    for (uint v = 0; same && v < a.num_nodes; ++v) same = a.selected[v] == b.selected[v];
+    for (uint e = 0; same && e < a.num_edges; ++e)
+        same = a.edges[e].source == b.edges[e].source && a.edges[e].end == b.edges[e].end &&
+               a.weights[e] == b.weights[e];
+    std::cout << (same ? "SAME" : "DIFFERENT") << " " << a.num_edges << std::endl;
+    UMVirtualGraph vg(b);
+    vg.MakeGraph();
+    std::cout << "PARTS " << vg.numParts << std::endl;
+    return same ? 0 : 1;
+}
+'''
+
+
+def test_um_vertex_subgraph_equals_vertex_subgraph(tmp_path):
+    """UMVertexSubgraph (managed-memory twin) keeps the same vertices and edges as VertexSubgraph for the
+    same seed, and its result builds a UMVirtualGraph."""
+    import shutil
+
+    import eegraph_gb300 as E
+
+    if shutil.which("g++") is None:
+        pytest.skip("needs a C++ compiler")
+    s, d, w = E.gen_rmat(10, 8, seed=61, wmin=1, wmax=63)
+    g = tmp_path / "g.wel"
+    _write_wel(g, s, d, w)
+    src = tmp_path / "drv.cpp"
+    src.write_text(UM_SUB_DRIVER)
+    exe = tmp_path / "drv"
+    lib = ROOT / "eegraph_gb300" / "_lib"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-o", str(exe), str(src), "-I", str(ROOT / "include"),
+                    "-L", str(lib), "-leegraph_facade", "-leegraph", f"-Wl,-rpath,{lib}", "-pthread"],
+                   check=True, timeout=180)
+    r = subprocess.run([str(exe), str(g)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "SAME" in r.stdout and "PARTS " in r.stdout
