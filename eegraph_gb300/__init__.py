@@ -577,6 +577,23 @@ class PPR:
             pass
 
 
+def shard_queries(costs, world: int) -> list[list[int]]:
+    """Static partition of independent queries over `world` GPUs by estimated work (largest first onto the
+    least-loaded GPU; ties to the lower rank). Every rank computes the same partition from the same costs,
+    so no exchange is needed; each shard keeps its queries in input order."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    costs = [float(c) for c in costs]
+    order = sorted(range(len(costs)), key=lambda i: (-costs[i], i))
+    load = [0.0] * world
+    shards: list[list[int]] = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        shards[r].append(i)
+        load[r] += costs[i]
+    return [sorted(sh) for sh in shards]
+
+
 def autotune_k(num_nodes: int, src, dst, w=None, reps: int = 3):
     """Fastest part size K for this graph (BFS + SSSP from the max-degree vertex); (K, ms per K)."""
     src, dst = _u32(src), _u32(dst)
