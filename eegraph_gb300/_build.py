@@ -3,7 +3,8 @@
 Compiles every CUDA translation unit for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a -lineinfo``), the host C++ units with g++, links
 ``eegraph_gb300/_lib/libeegraph.so`` (static cudart, so the only runtime dependency is the driver)
-and the per-algorithm executables ``eegraph_gb300/_bin/{bfs,sssp,sswp,cc,pr}-main``.
+and the executables in ``eegraph_gb300/_bin/``: the per-algorithm programs ``{bfs,sssp,sswp,cc,pr}-main``,
+``sweep-main``, ``graph-info-main`` and ``converter``.
 Objects are rebuilt only when a source or header is newer. Sources compile in parallel.
 """
 from __future__ import annotations
@@ -81,7 +82,8 @@ def build(verbose: bool = False, jobs: int | None = None, verbose_ptxas: bool = 
     units = [(CSRC / s, OBJ / (Path(s).stem + ".o")) for s in CU_SOURCES + CPP_SOURCES]
     fac = [(CSRC / s, OBJ / ("facade_" + Path(s).stem + ".o")) for s in FACADE_SOURCES]
     cli = [(CSRC / "cli" / "main.cpp", OBJ / "cli_main.o"), (CSRC / "cli" / "sweep.cpp", OBJ / "cli_sweep.o"),
-           (CSRC / "cli" / "graph_info.cpp", OBJ / "cli_graph_info.o")]
+           (CSRC / "cli" / "graph_info.cpp", OBJ / "cli_graph_info.o"),
+           (CSRC / "cli" / "converter.cpp", OBJ / "cli_converter.o")]
     jobs = jobs or max(2, min(16, os.cpu_count() or 2))
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_compile, s, o, hdrs, verbose_ptxas) for s, o in units + fac + cli]
@@ -109,6 +111,11 @@ def build(verbose: bool = False, jobs: int | None = None, verbose_ptxas: bool = 
         if _stale(target, [obj, fac_lib, lib]):
             _run(["g++", "-o", str(target), str(obj), "-L", str(LIB),
                   "-leegraph_facade", "-leegraph", "-Wl,-rpath,$ORIGIN/../_lib", "-pthread"])
+    # Subway's text-to-binary CSR converter (C ABI only)
+    target = BIN / "converter"
+    if _stale(target, [cli[3][1], lib]):
+        _run(["g++", "-o", str(target), str(cli[3][1]), "-L", str(LIB), "-leegraph", "-Wl,-rpath,$ORIGIN/../_lib",
+              "-pthread"])
     return lib
 
 

@@ -1,5 +1,5 @@
-"""Experiment tools of the reference on the C++ facade (CPU only): graph-info-main (src/graph_info.cpp)
-and VertexSubgraph::MakeSubgraph (src/graph.cpp:122-203)."""
+"""Experiment tools of the reference on the C++ facade (CPU only): graph-info-main (src/graph_info.cpp),
+VertexSubgraph::MakeSubgraph (src/graph.cpp:122-203) and Subway's converter (Subway/tools/converter.cpp)."""
 import ctypes
 import shutil
 import subprocess
@@ -91,3 +91,43 @@ def test_vertex_subgraph_selection_and_induced_edges(tmp_path):
     want_edges = [(a, b, c) for a, b, c in zip(s.tolist(), d.tolist(), w.tolist()) if a in sel and b in sel]
     assert got_edges == want_edges
     assert "Subgraph number of edges = %d" % len(want_edges) in r.stdout
+
+
+def _subway_csr(src, dst, w):
+    """Subway/tools/converter.cpp:38-94 (.el) and :95-165 (.wel), restated: num_nodes = largest id + 1,
+    offsets by counting, edges of a source in input order."""
+    n = int(max(src.max(), dst.max())) + 1 if src.size else 1
+    deg = np.bincount(src, minlength=n)
+    ptr = np.concatenate([[0], np.cumsum(deg)[:-1]]).astype(np.uint32)
+    order = np.argsort(src, kind="stable")
+    rec = dst[order] if w is None else np.stack([dst[order], w[order]], 1).reshape(-1)
+    return np.concatenate([[n, src.size], ptr, rec]).astype(np.uint32)
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+@pytest.mark.parametrize("one_based", [False, True])
+def test_converter_matches_subway_layout(tmp_path, weighted, one_based):
+    rng = np.random.default_rng(11)
+    n, m = 300, 4000
+    s = rng.integers(1 if one_based else 0, n, m)
+    d = rng.integers(1 if one_based else 0, n, m)
+    w = rng.integers(1, 1000, m)
+    p = tmp_path / ("g.wel" if weighted else "g.el")
+    with open(p, "w") as f:
+        for i in range(m):
+            f.write(f"{s[i]} {d[i]} {w[i]}\n" if weighted else f"{s[i]} {d[i]}\n")
+    r = subprocess.run([str(BIN / "converter"), str(p)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = tmp_path / ("g.bwcsr" if weighted else "g.bcsr")
+    got = np.fromfile(out, np.uint32)
+    want = _subway_csr(s.astype(np.uint32), d.astype(np.uint32), w.astype(np.uint32) if weighted else None)
+    assert np.array_equal(got, want)
+
+
+def test_converter_messages(tmp_path):
+    (tmp_path / "g.txt").write_text("0 1\n")
+    r = subprocess.run([str(BIN / "converter"), str(tmp_path / "g.txt")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "Input file format is not supported." in r.stdout
+    assert not (tmp_path / "g.bcsr").exists()
+    r = subprocess.run([str(BIN / "converter")], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "There was an error parsing command line arguments" in r.stdout
