@@ -478,18 +478,29 @@ def ppr_cpu_baseline(budget_s: float, scale: int = 14, cols: int = 64) -> dict:
 
 def bench_ppr(args) -> None:
     """Differentiable personalised PageRank: forward + adjoint + gradients for 64 teleport vectors in
-    one batched call pair, against the single-column kernels looped per teleport vector."""
+    one batched call pair, against the single-column kernels looped per teleport vector. With N GPUs
+    (torchrun) the columns are split (eegraph_gb300.shard_columns): each GPU solves its columns on the
+    whole graph and the per-edge gradients are summed across GPUs with one all-reduce of 2m floats
+    inside the timed step; the job's time is the slowest GPU's (strong scaling: the total is fixed)."""
     import torch
 
     import eegraph_gb300 as E
 
     rank, world, local = dist_env()
-    if rank != 0:
-        return
     torch.cuda.set_device(local)
     E.lib().eeg_set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
     scale = args.scale if args.scale != SCALE else PPR_SCALE
-    n, s, d, w, T, G = make_ppr_inputs(E, scale)
+    n, s, d, w, T_all, G_all = make_ppr_inputs(E, scale, cols=args.ppr_columns)
+    C_all = T_all.shape[1]
+    cols = E.shard_columns(C_all, world)[rank]
+    if not cols:
+        raise SystemExit(f"rank {rank}: no columns (more GPUs than the {C_all} columns)")
+    T, G = np.ascontiguousarray(T_all[:, cols]), np.ascontiguousarray(G_all[:, cols])
     C = T.shape[1]
     m = int(s.size)
     stream = torch.cuda.current_stream().cuda_stream
@@ -498,8 +509,8 @@ def bench_ppr(args) -> None:
     Tt, Gt = torch.from_numpy(T).to(dev), torch.from_numpy(G).to(dev)
     X = torch.empty_like(Tt)
     dT = torch.empty_like(Tt)
-    dw = torch.empty(m, dtype=torch.float32, device=dev)
-    dwn = torch.empty(m, dtype=torch.float32, device=dev)
+    grads = torch.empty(2 * m, dtype=torch.float32, device=dev)  # dLoss/dw and dLoss/dW, reduced together
+    dw, dwn = grads[:m], grads[m:]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     outs = {"dw": dw.data_ptr(), "dwn": dwn.data_ptr(), "dt": dT.data_ptr()}
@@ -515,6 +526,8 @@ def bench_ppr(args) -> None:
             ev0.record()
             _, rf = pb.forward(Tt.data_ptr(), X.data_ptr(), stream=stream)
             _, ra = pb.adjoint(Gt.data_ptr(), out_ptrs=outs, stream=stream)
+            if dist is not None:
+                dist.all_reduce(grads)  # the batch's edge gradients: the sum over the GPUs' columns
             ev1.record()
             torch.cuda.synchronize()
             if i >= args.warmup:
@@ -522,7 +535,7 @@ def bench_ppr(args) -> None:
                 fwd.append(rf)
                 adj.append(ra)
         energy_line = energy.summary(args.steps, "timed steps (with their L2 flushes)")
-        Xb, dwb, dTb = X.cpu().numpy(), dw.cpu().numpy(), dT.cpu().numpy()
+        # duality c^T x = (1-d) t^T lambda over this GPU's columns
         duality = abs(float((Gt.double() * X.double()).sum()) - float((Tt.double() * dT.double()).sum()))
         duality /= float((Gt.double() * X.double()).abs().sum())
         # end to end through the host API: pinned host inputs in, gradients out to host
@@ -534,7 +547,13 @@ def bench_ppr(args) -> None:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             pb.forward(Th.numpy(), False, stream=stream)
-            pb.adjoint(Gh.numpy(), out_host={"dw": dw_h.numpy(), "dt": dT_h.numpy()}, stream=stream)
+            if dist is None:
+                pb.adjoint(Gh.numpy(), out_host={"dw": dw_h.numpy(), "dt": dT_h.numpy()}, stream=stream)
+            else:  # the edge gradients are summed on the devices, then read back
+                pb.adjoint(Gh.numpy(), out_ptrs={"dw": dw.data_ptr(), "dt": dT.data_ptr()}, stream=stream)
+                dist.all_reduce(dw)
+                dw_h.copy_(dw)
+                dT_h.copy_(dT)
             torch.cuda.synchronize()
             if i >= args.warmup:
                 e2e_ms.append((time.perf_counter() - t0) * 1e3)
@@ -561,41 +580,59 @@ def bench_ppr(args) -> None:
                     loop_ms.append(ev0.elapsed_time(ev1))
         def nl1(a, b):
             return float((a - b).abs().sum() / b.abs().sum())
+        if dist is not None:
+            dist.all_reduce(dw1)  # the loop's edge gradients over all GPUs' columns, as the batch's
         parity = {"X_nl1": nl1(Xc.t().double(), X.double()), "dT_nl1": nl1(dTc.t().double(), dT.double()),
                   "dw_rel_l1": nl1(dw1.double(), dw.double()), "duality_rel": duality}
     vg.close()
-    bms = statistics.median(step_ms)
-    lms = statistics.median(loop_ms)
+
+    def job_max(x):  # the slowest (or worst) GPU's figure
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t[0])
+
+    bms = job_max(statistics.median(step_ms))
+    lms = job_max(statistics.median(loop_ms))
+    e2e_med = job_max(statistics.median(e2e_ms)) if e2e_ms else None
+    parity = {k: job_max(v) for k, v in parity.items()}
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return
     fkm = statistics.median(r["kernel_ms"] for r in fwd)
     fby = statistics.median(r["algorithmic_bytes"] for r in fwd)
     fit = int(statistics.median(r["iterations"] for r in fwd))
     ait = int(statistics.median(r["iterations"] for r in adj))
     peak, peak_kind = load_peaks()
     ach = fby / (fkm * 1e-3) / 1e9
-    h2d = 2 * n * C * 4
-    d2h = m * 4 + n * C * 4
+    h2d = 2 * n * C_all * 4                     # all GPUs: their teleport and dLoss/dX columns
+    d2h = world * m * 4 + n * C_all * 4         # each GPU reads the summed dLoss/dw and its dLoss/dT columns
     line = {
         "metric": "PR-grad/s (personalised PageRank forward + implicit adjoint + edge/teleport gradients, "
                   "teleport vectors per second)",
-        "value": round(C / (bms * 1e-3), 2), "unit": "PR-grad/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(bms, 3), "higher_is_better": True, "scaling": "weak",
+        "value": round(C_all / (bms * 1e-3), 2), "unit": "PR-grad/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(bms, 3), "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32 (FP64 stop-test reduction)",
         "data": "synthetic (seeded R-MAT, weights U(0,1], teleports and c generated in-process)",
-        "config": {"workload": f"R-MAT s{scale} ef{EF}, {C} teleport vectors x {PPR_SEEDS} seeds, d=0.85, "
-                               f"tol 1e-7, K={args.k}", "vertices": n, "edges": m, "columns": C,
-                   "l2": "iterates 2 x n x 64 x 4 B larger than L2; 256 MB L2 flush between timed steps"},
+        "config": {"workload": f"R-MAT s{scale} ef{EF}, {C_all} teleport vectors x {PPR_SEEDS} seeds, d=0.85, "
+                               f"tol 1e-7, K={args.k}", "vertices": n, "edges": m, "columns": C_all,
+                   "row_width": 1 if C == 1 else (32 if C <= 32 else 64),
+                   "parallelism": f"columns split over {world} GPU(s) ({C} on rank 0), edge gradients all-reduced",
+                   "l2": "iterates 2 x n x row width x 4 B larger than L2; 256 MB L2 flush between timed steps"},
         "sweeps": {"forward": fit, "adjoint": ait},
-        "plain_loop": {"ms_per_step": round(lms, 3), "grads_per_s": round(C / (lms * 1e-3), 2)},
+        "plain_loop": {"ms_per_step": round(lms, 3), "grads_per_s": round(C_all / (lms * 1e-3), 2)},
         "speedup_vs_plain_loop": round(lms / bms, 2),
         "parity_batched_vs_loop": parity,
         "roofline": {"bound": "hbm", "kernel": "k_ppr_rows (forward solve)", "achieved": round(ach, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                     "traffic": load_traffic("k_ppr_rows", f"ppr_s{scale}_k{args.k}"),
-                     "note": "algorithmic bytes count every 256-B row gather as DRAM traffic; about 79 % of "
-                             "them hit L2 (traffic = measured DRAM bytes per launch), so frac can exceed 1"},
-        "e2e": {"value": round(C / (statistics.median(e2e_ms) * 1e-3), 2) if e2e_ms else None, "unit": "PR-grad/s",
+                     "traffic": load_traffic("k_ppr_rows", f"ppr_s{scale}_k{args.k}") if C > 32 else None,
+                     "note": "algorithmic bytes count every row gather as DRAM traffic; at 64 columns about "
+                             "79 % of them hit L2 (traffic = measured DRAM bytes per launch), so frac can exceed 1"},
+        "e2e": {"value": round(C_all / (e2e_med * 1e-3), 2) if e2e_med else None, "unit": "PR-grad/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(statistics.median(e2e_ms), 3) if e2e_ms else None},
+                "ms_per_step": round(e2e_med, 3) if e2e_med else None},
         "gpu_launches": 5,
         "clocks": clk.summary(),
         "energy": energy_line,
@@ -805,6 +842,7 @@ def main() -> None:
                          "batch: 256-graph query mixture, batched vs looped; "
                          "ppr: personalised PageRank forward + adjoint, 64 teleport vectors, batched vs looped")
     ap.add_argument("--batch-graphs", type=int, default=256)
+    ap.add_argument("--ppr-columns", type=int, default=PPR_COLS, help="teleport vectors of the ppr workload (1-64)")
     ap.add_argument("--grid-side", type=int, default=GRID_SIDE)
     ap.add_argument("--grid-delta-sssp", type=int, default=8000, help="SSSP bucket width on the grid (0 = plain)")
     ap.add_argument("--grid-delta-sswp", type=int, default=16, help="SSWP bucket width on the grid (0 = plain)")

@@ -577,6 +577,21 @@ class PPR:
             pass
 
 
+def shard_columns(columns: int, world: int) -> list[list[int]]:
+    """Contiguous split of a personalised-PageRank column batch over `world` GPUs (sizes differ by at
+    most one). Each GPU solves its columns on the whole graph; the batch's edge gradients are the sum
+    of the GPUs' (one reduction of m floats), its X and dLoss/dT the concatenation."""
+    if world < 1 or columns < 1:
+        raise ValueError("columns and world must be >= 1")
+    base, extra = divmod(columns, world)
+    out, c = [], 0
+    for r in range(world):
+        k = base + (1 if r < extra else 0)
+        out.append(list(range(c, c + k)))
+        c += k
+    return out
+
+
 def shard_queries(costs, world: int) -> list[list[int]]:
     """Static partition of independent queries over `world` GPUs by estimated work (largest first onto the
     least-loaded GPU; ties to the lower rank). Every rank computes the same partition from the same costs,

@@ -14,9 +14,9 @@
 // its own. Each hub chunk writes a partial; the last chunk of a group of 32 to arrive sums the group
 // (compensated FP32, in chunk order) and the last group sums the groups. Deterministic, and a sweep
 // needs one grid barrier (Jacobi, double-buffered iterates).
-//   Batched rows (2..64 columns; rows padded to 64 FP32 = 256 B): a warp owns a chunk; half-warp h
-//   takes slots h, h+2, ... of each part and lane q the float4 of columns 4q..4q+3, so one gather
-//   instruction moves two 256-B rows, with 8 rows per lane in flight.
+//   Batched rows (2..64 columns; rows padded to W = 32 or 64 FP32, 128 or 256 B): a warp owns a chunk and
+//   splits into G = 128/W lane groups of W/4 lanes; group g takes slots g, g+G, ... of each part and
+//   lane q of a group the float4 of columns 4q..4q+3, so one gather instruction moves G rows.
 //   Single column (the plain form): a lane owns a slot; part sums by K-lane butterflies, vertex sums by
 //   a segmented warp scan.
 // Stop test: d/(1-d) * ||Y_{k+1}-Y_k||_1 <= tol * ||Y_{k+1}||_1 over all columns, reduced in FP64
@@ -33,7 +33,7 @@ namespace {
 
 constexpr uint32_t PPR_SLOTS = 128;  // slots per work chunk
 constexpr uint32_t PPR_GROUP = 32;   // hub chunks per first-level group
-constexpr uint32_t PPR_W = 64;       // row width of the batched form (FP32 columns)
+constexpr uint32_t PPR_W = 64;       // widest row of the batched form (FP32 columns)
 constexpr int PPR_TPB = 256;
 constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr unsigned FULL = 0xFFFFFFFFu;
@@ -126,14 +126,14 @@ __device__ __forceinline__ T pick(const T (&a)[N], uint32_t j) {
     return r;
 }
 
-// Half-warp transpose reduction: each lane holds N values (one per slot of its half); afterwards lane
-// q holds the sum over the 16 lanes of the half of value index(q) (see red_index). log2(N) halving
-// steps, then plain butterflies.
-template <int N>
+// Lane-group transpose reduction: each lane holds N values (one per slot of its group of NQ lanes);
+// afterwards lane q holds the sum over the group's lanes of value index(q) (see red_index). log2(N)
+// halving steps, then plain butterflies.
+template <int N, int NQ>
 __device__ __forceinline__ float tred(float (&v)[N], uint32_t q) {
     int n = N;
 #pragma unroll
-    for (int o = 8; o >= 1; o >>= 1) {
+    for (int o = NQ / 2; o >= 1; o >>= 1) {
         if (n >= 2) {
             const bool up = (q & (uint32_t)o) != 0;
 #pragma unroll
@@ -151,12 +151,12 @@ __device__ __forceinline__ float tred(float (&v)[N], uint32_t q) {
     }
     return v[0];
 }
-template <int N>
+template <int N, int NQ>
 __device__ __forceinline__ uint32_t red_index(uint32_t q) {
     uint32_t i = 0;
     int n = N;
 #pragma unroll
-    for (int o = 8; o >= 1; o >>= 1) {
+    for (int o = NQ / 2; o >= 1; o >>= 1) {
         if (n >= 2) {
             if (q & (uint32_t)o) i += (uint32_t)(n / 2);
             n >>= 1;
@@ -165,23 +165,100 @@ __device__ __forceinline__ uint32_t red_index(uint32_t q) {
     return i;
 }
 
-// Compensated sum of partial rows [first, first+cnt) (width 64 = 16 float4); half-warps take
-// alternate rows; every lane of the warp returns the same float4 for its q.
-__device__ float4 sum_rows(const float4* base, uint32_t first, uint32_t cnt, uint32_t half, uint32_t q) {
+// Sum of a float4 over the warp's lane groups (lanes q, q+NQ, ...); every lane gets its q's total.
+template <int NQ>
+__device__ __forceinline__ float4 across_groups(float4 v) {
+#pragma unroll
+    for (int o = NQ; o < 32; o <<= 1) v = add4(v, shfl_xor4(v, o));
+    return v;
+}
+
+// Compensated sum of partial rows [first, first+cnt) (NQ float4 each); lane groups take rows in turn;
+// every lane of the warp returns the same float4 for its q.
+template <int NQ>
+__device__ float4 sum_rows(const float4* base, uint32_t first, uint32_t cnt, uint32_t grp, uint32_t q) {
+    constexpr uint32_t G = 32 / NQ;
     float4 hi = f4(0.f), lo = f4(0.f);
-    for (uint32_t i = half; i < cnt; i += 2) {
-        const float4 p = __ldcg(base + (size_t)(first + i) * 16u + q);
+    for (uint32_t i = grp; i < cnt; i += G) {
+        const float4 p = __ldcg(base + (size_t)(first + i) * NQ + q);
         pair_add(hi.x, lo.x, p.x, 0.f);
         pair_add(hi.y, lo.y, p.y, 0.f);
         pair_add(hi.z, lo.z, p.z, 0.f);
         pair_add(hi.w, lo.w, p.w, 0.f);
     }
-    const float4 ho = shfl_xor4(hi, 16), lo2 = shfl_xor4(lo, 16);
-    pair_add(hi.x, lo.x, ho.x, lo2.x);
-    pair_add(hi.y, lo.y, ho.y, lo2.y);
-    pair_add(hi.z, lo.z, ho.z, lo2.z);
-    pair_add(hi.w, lo.w, ho.w, lo2.w);
+#pragma unroll
+    for (int o = NQ; o < 32; o <<= 1) {
+        const float4 ho = shfl_xor4(hi, o), lo2 = shfl_xor4(lo, o);
+        pair_add(hi.x, lo.x, ho.x, lo2.x);
+        pair_add(hi.y, lo.y, ho.y, lo2.y);
+        pair_add(hi.z, lo.z, ho.z, lo2.z);
+        pair_add(hi.w, lo.w, ho.w, lo2.w);
+    }
     return hi;
+}
+
+// Slot j*G + grp of a part row (grp run-time, the array index compile-time: no local memory).
+template <int G, int K>
+__device__ __forceinline__ uint32_t group_slot(const uint32_t (&row)[K], int j, uint32_t grp) {
+    uint32_t r = row[j * G];
+#pragma unroll
+    for (int g = 1; g < G; ++g)
+        if (grp == (uint32_t)g) r = row[j * G + g];
+    return r;
+}
+
+// Rows gathered per lane per step: 8, so U = 8/H parts per step (16/K at W = 64, 32/K at W = 32).
+template <int K, int G>
+struct RowStep {
+    static constexpr int H = K / G;  // slots of a part per lane group
+    static constexpr int U = 8 / H;  // parts per step
+};
+
+// Neighbour ids and weights of this lane group's slots (j*G + grp) of parts pp .. pp+U-1 of a chunk
+// (NONE and 0 past its np parts). Two groups (W = 64): whole rows by 256-bit loads, then a selection;
+// more groups: the group's slots one by one (the whole rows would take 2*U*K registers).
+template <int K, int G>
+__device__ __forceinline__ void load_group_slots(const DirTab& g, uint32_t p0, uint32_t pp, uint32_t np, uint32_t grp,
+                                                 uint64_t pol, uint32_t (&colg)[RowStep<K, G>::U][K / G],
+                                                 uint32_t (&wbg)[RowStep<K, G>::U][K / G]) {
+    constexpr int U = RowStep<K, G>::U, H = K / G;
+    if constexpr (G <= 2) {
+        uint32_t col[U][K], wb[U][K];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            if (pp + u < np) {
+                const size_t row = (size_t)(p0 + pp + u) * K;
+                ld_part<K>(g.vcol + row, col[u], pol);
+                ld_part<K>(reinterpret_cast<const uint32_t*>(g.w) + row, wb[u], pol);
+            } else {
+#pragma unroll
+                for (int j = 0; j < K; ++j) {
+                    col[u][j] = NONE;
+                    wb[u][j] = 0u;
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+                colg[u][j] = group_slot<G>(col[u], j, grp);
+                wbg[u][j] = group_slot<G>(wb[u], j, grp);
+            }
+    } else {
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < H; ++j) {
+                colg[u][j] = NONE;
+                wbg[u][j] = 0u;
+                if (pp + u < np) {
+                    const size_t at = (size_t)(p0 + pp + u) * K + (size_t)(j * G) + grp;
+                    colg[u][j] = ld_nc(g.vcol + at);
+                    wbg[u][j] = __float_as_uint(__ldg(g.w + at));
+                }
+            }
+    }
 }
 // Compensated sum of scalar partials [first, first+cnt); all lanes return the same value.
 __device__ float sum_scalars(const float* base, uint32_t first, uint32_t cnt, uint32_t lane) {
@@ -218,37 +295,38 @@ __device__ __forceinline__ uint32_t next_chunk(uint32_t* ctr, uint32_t nchunks, 
     return c < nchunks ? (uint32_t)c : NONE;
 }
 
-// Hub chunk delivery, batched rows. `tot` is the chunk's row (same in both halves). Returns true in
-// the warp that completes the hub for this sweep (`mult` = sweeps completed including this one), with
+// Hub chunk delivery, batched rows. `tot` is the chunk's row (same in every lane group). Returns true
+// in the warp that completes the hub for this sweep (`mult` = sweeps completed including this one), with
 // the hub's full row in `out` and its vertex in `v`. Warp-collective.
+template <int NQ>
 __device__ bool hub_rows(const DirTab& g, const Chunk& ch, const float4& tot, uint32_t mult, uint32_t lane,
                          float4& out, uint32_t& v) {
-    const uint32_t half = lane >> 4, q = lane & 15u;
+    const uint32_t grp = lane / NQ, q = lane % NQ;
     const Hub H = g.hub[ch.hub];
     float4* part = reinterpret_cast<float4*>(g.partial);
     float4* gpart = reinterpret_cast<float4*>(g.gpartial);
-    if (half == 0) {
-        part[(size_t)(H.first + ch.idx) * 16u + q] = tot;
+    if (grp == 0) {
+        part[(size_t)(H.first + ch.idx) * NQ + q] = tot;
         __threadfence();
     }
     __syncwarp();
     const uint32_t gi = ch.idx / PPR_GROUP, g0 = gi * PPR_GROUP;
     const uint32_t gs = min(PPR_GROUP, H.count - g0);
     if (!arrive_last(&g.garrive[H.gfirst + gi], mult * gs, lane)) return false;
-    const float4 s1 = sum_rows(part, H.first + g0, gs, half, q);
+    const float4 s1 = sum_rows<NQ>(part, H.first + g0, gs, grp, q);
     const uint32_t ng = (H.count + PPR_GROUP - 1) / PPR_GROUP;
     v = H.v;
     if (ng == 1) {
         out = s1;
         return true;
     }
-    if (half == 0) {
-        gpart[(size_t)(H.gfirst + gi) * 16u + q] = s1;
+    if (grp == 0) {
+        gpart[(size_t)(H.gfirst + gi) * NQ + q] = s1;
         __threadfence();
     }
     __syncwarp();
     if (!arrive_last(&g.harrive[ch.hub], mult * ng, lane)) return false;
-    out = sum_rows(gpart, H.gfirst, ng, half, q);
+    out = sum_rows<NQ>(gpart, H.gfirst, ng, grp, q);
     return true;
 }
 // Same for one scalar per chunk.
@@ -312,25 +390,27 @@ __device__ __forceinline__ int end_sweep(const SolveArgs& a, uint32_t s, double 
 }
 
 // ------------------------------------------------------------------ batched rows: solve
-template <int K>
+template <int NQ>
 __device__ __forceinline__ void flush_row(const SolveArgs& a, float4* out, uint32_t v, float4 acc, const float4& bv,
-                                          const float4& ov, uint32_t half, uint32_t q, float& rr, float& nn) {
-    acc = add4(acc, shfl_xor4(acc, 16));
+                                          const float4& ov, uint32_t grp, uint32_t q, float& rr, float& nn) {
+    acc = across_groups<NQ>(acc);
     const float4 y = affine4(a.d, acc, a.scale_b, bv);
-    if (half == 0) {
-        out[(size_t)v * 16u + q] = y;
+    if (grp == 0) {
+        out[(size_t)v * NQ + q] = y;
         rr += l1diff4(y, ov);
         nn += l14(y);
     }
 }
 
 // 3 CTAs per SM (<= 85 registers, a few spilled): the solve is latency-bound, and 24 warps per SM
-// instead of 16 measured 1.3x faster on R-MAT s20 x 64 columns.
-template <int K>
+// instead of 16 measured 1.3x faster on R-MAT s20 x 64 columns. NQ = W/4 lanes per row.
+template <int K, int NQ>
 __global__ void __launch_bounds__(PPR_TPB, 3) k_ppr_rows(SolveArgs a) {
-    constexpr int U = K >= 16 ? 1 : 16 / K;  // parts per step: 8 row gathers in flight per lane
-    constexpr int H = K / 2;                 // slots per half-warp per part
-    const uint32_t lane = threadIdx.x & 31u, half = lane >> 4, q = lane & 15u;
+    constexpr int G = 32 / NQ;               // lane groups (rows per gather instruction)
+    constexpr int H = K / G;                 // slots per group per part
+    constexpr int U = RowStep<K, G>::U;      // parts per step: 8 row gathers in flight per lane
+    static_assert(H >= 1 && H <= 8, "K must be at least the number of lane groups");
+    const uint32_t lane = threadIdx.x & 31u, grp = lane / NQ, q = lane % NQ;
     __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
     if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
     __syncthreads();
@@ -341,7 +421,7 @@ __global__ void __launch_bounds__(PPR_TPB, 3) k_ppr_rows(SolveArgs a) {
     {
         float4* y0 = reinterpret_cast<float4*>(a.y0);
         float4* y1 = reinterpret_cast<float4*>(a.y1);
-        const uint64_t tot = (uint64_t)a.n * 16u;
+        const uint64_t tot = (uint64_t)a.n * NQ;
         for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < tot;
              i += (uint64_t)gridDim.x * blockDim.x) {
             const float4 v = b[i];
@@ -361,62 +441,48 @@ __global__ void __launch_bounds__(PPR_TPB, 3) k_ppr_rows(SolveArgs a) {
             const uint32_t np = ch.p1 - ch.p0;
             const uint32_t own_l = lane < np ? ld_nc(a.g.vowner + ch.p0 + lane) : NONE;
             uint32_t cur = __shfl_sync(FULL, own_l, 0);
-            float4 bv = b[(size_t)cur * 16u + q];
-            float4 ov = in[(size_t)cur * 16u + q];
+            float4 bv = b[(size_t)cur * NQ + q];
+            float4 ov = in[(size_t)cur * NQ + q];
             float4 acc = f4(0.f);
             float rr = 0.f, nn = 0.f;
             for (uint32_t pp = 0; pp < np; pp += U) {
-                uint32_t col[U][K], wb[U][K];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (pp + u < np) {
-                        const size_t row = (size_t)(ch.p0 + pp + u) * K;
-                        ld_part<K>(a.g.vcol + row, col[u], pol);
-                        ld_part<K>(reinterpret_cast<const uint32_t*>(a.g.w) + row, wb[u], pol);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < K; ++j) {
-                            col[u][j] = NONE;
-                            wb[u][j] = 0u;
-                        }
-                    }
-                }
+                uint32_t colg[U][H], wbg[U][H];
+                load_group_slots<K, G>(a.g, ch.p0, pp, np, grp, pol, colg, wbg);
                 float4 xv[U][H];
 #pragma unroll
                 for (int u = 0; u < U; ++u)
 #pragma unroll
                     for (int j = 0; j < H; ++j) {
-                        const uint32_t id = half ? col[u][2 * j + 1] : col[u][2 * j];
-                        xv[u][j] = id != NONE ? in[(size_t)id * 16u + q] : f4(0.f);
+                        const uint32_t id = colg[u][j];
+                        xv[u][j] = id != NONE ? in[(size_t)id * NQ + q] : f4(0.f);
                     }
 #pragma unroll
                 for (int u = 0; u < U; ++u) {
                     if (pp + u < np) {
                         const uint32_t o = __shfl_sync(FULL, own_l, pp + u);
                         if (o != cur) {
-                            flush_row<K>(a, out, cur, acc, bv, ov, half, q, rr, nn);
+                            flush_row<NQ>(a, out, cur, acc, bv, ov, grp, q, rr, nn);
                             acc = f4(0.f);
                             cur = o;
-                            bv = b[(size_t)cur * 16u + q];
-                            ov = in[(size_t)cur * 16u + q];
+                            bv = b[(size_t)cur * NQ + q];
+                            ov = in[(size_t)cur * NQ + q];
                         }
 #pragma unroll
-                        for (int j = 0; j < H; ++j)
-                            fma4(acc, __uint_as_float(half ? wb[u][2 * j + 1] : wb[u][2 * j]), xv[u][j]);
+                        for (int j = 0; j < H; ++j) fma4(acc, __uint_as_float(wbg[u][j]), xv[u][j]);
                     }
                 }
             }
             if (ch.hub == NONE) {
-                flush_row<K>(a, out, cur, acc, bv, ov, half, q, rr, nn);
+                flush_row<NQ>(a, out, cur, acc, bv, ov, grp, q, rr, nn);
             } else {
-                const float4 tot = add4(acc, shfl_xor4(acc, 16));
+                const float4 tot = across_groups<NQ>(acc);
                 float4 full;
                 uint32_t v;
-                if (hub_rows(a.g, ch, tot, s + 1, lane, full, v)) {
-                    const float4 y = affine4(a.d, full, a.scale_b, b[(size_t)v * 16u + q]);
-                    if (half == 0) {
-                        const float4 o = in[(size_t)v * 16u + q];
-                        out[(size_t)v * 16u + q] = y;
+                if (hub_rows<NQ>(a.g, ch, tot, s + 1, lane, full, v)) {
+                    const float4 y = affine4(a.d, full, a.scale_b, b[(size_t)v * NQ + q]);
+                    if (grp == 0) {
+                        const float4 o = in[(size_t)v * NQ + q];
+                        out[(size_t)v * NQ + q] = y;
                         rr += l1diff4(y, o);
                         nn += l14(y);
                     }
@@ -540,50 +606,39 @@ finish:
 
 // ------------------------------------------------------------------ gradients
 // Batched rows: g_uv = d <X_u, L_v> per forward slot; r_u = sum_v g_uv W_uv per vertex.
-template <int K>
+template <int K, int NQ>
 __global__ void __launch_bounds__(PPR_TPB, 2) k_ppr_grad_rows(GradArgs a) {
-    constexpr int U = K >= 16 ? 1 : 16 / K;
-    constexpr int H = K / 2;
-    const uint32_t lane = threadIdx.x & 31u, half = lane >> 4, q = lane & 15u;
+    constexpr int G = 32 / NQ;
+    constexpr int H = K / G;
+    constexpr int U = RowStep<K, G>::U;
+    static_assert(H >= 1 && H <= NQ, "K must be at least the number of lane groups");
+    const uint32_t lane = threadIdx.x & 31u, grp = lane / NQ, q = lane % NQ;
     __shared__ uint32_t s_next[2];  // per sweep (alternating): next of this CTA's chunks
     if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
     __syncthreads();
     const uint64_t pol = l2_evict_first_policy();
     const float4* X = reinterpret_cast<const float4*>(a.X);
     const float4* L = reinterpret_cast<const float4*>(a.L);
-    const uint32_t ri = red_index<H>(q);
-    const uint32_t jme = 2u * ri + half;                       // slot this lane reports after the reduction
-    const bool writer = (q & (uint32_t)(16 / H - 1)) == 0u;    // one lane per reduced value
+    const uint32_t ri = red_index<H, NQ>(q);
+    const uint32_t jme = (uint32_t)G * ri + grp;               // slot this lane reports after the reduction
+    const bool writer = (q & (uint32_t)(NQ / H - 1)) == 0u;    // one lane per reduced value
     for (uint32_t c; (c = next_chunk(&s_next[0], a.g.nchunks, lane)) != NONE;) {
         const Chunk ch = a.g.chunk[c];
         const uint32_t np = ch.p1 - ch.p0;
         const uint32_t own_l = lane < np ? ld_nc(a.g.vowner + ch.p0 + lane) : NONE;
         uint32_t cur = __shfl_sync(FULL, own_l, 0);
-        float4 xu = X[(size_t)cur * 16u + q];
+        float4 xu = X[(size_t)cur * NQ + q];
         float racc = 0.f;
         for (uint32_t pp = 0; pp < np; pp += U) {
-            uint32_t col[U][K], wb[U][K];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                if (pp + u < np) {
-                    const size_t row = (size_t)(ch.p0 + pp + u) * K;
-                    ld_part<K>(a.g.vcol + row, col[u], pol);
-                    ld_part<K>(reinterpret_cast<const uint32_t*>(a.g.w) + row, wb[u], pol);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < K; ++j) {
-                        col[u][j] = NONE;
-                        wb[u][j] = 0u;
-                    }
-                }
-            }
+            uint32_t colg[U][H], wbg[U][H];
+            load_group_slots<K, G>(a.g, ch.p0, pp, np, grp, pol, colg, wbg);
             float4 lv[U][H];
 #pragma unroll
             for (int u = 0; u < U; ++u)
 #pragma unroll
                 for (int j = 0; j < H; ++j) {
-                    const uint32_t id = half ? col[u][2 * j + 1] : col[u][2 * j];
-                    lv[u][j] = id != NONE ? L[(size_t)id * 16u + q] : f4(0.f);
+                    const uint32_t id = colg[u][j];
+                    lv[u][j] = id != NONE ? L[(size_t)id * NQ + q] : f4(0.f);
                 }
 #pragma unroll
             for (int u = 0; u < U; ++u) {
@@ -596,18 +651,18 @@ __global__ void __launch_bounds__(PPR_TPB, 2) k_ppr_grad_rows(GradArgs a) {
                         if (lane == 0) a.r[cur] = a.accumulate ? a.r[cur] + t : t;
                         racc = 0.f;
                         cur = o;
-                        xu = X[(size_t)cur * 16u + q];
+                        xu = X[(size_t)cur * NQ + q];
                     }
                     float dv[H];
 #pragma unroll
                     for (int j = 0; j < H; ++j) dv[j] = dot4(xu, lv[u][j]);
-                    const float dsum = tred<H>(dv, q);
-                    const uint32_t id = pick<K>(col[u], jme);
+                    const float dsum = tred<H, NQ>(dv, q);
+                    const uint32_t id = pick<H>(colg[u], ri);  // slot jme of the part
                     if (writer && id != NONE) {
                         const float g = a.d * dsum;
                         const size_t slot = (size_t)(ch.p0 + pp + u) * K + jme;
                         a.gslot[slot] = a.accumulate ? a.gslot[slot] + g : g;
-                        racc = fmaf(g, __uint_as_float(pick<K>(wb[u], jme)), racc);
+                        racc = fmaf(g, __uint_as_float(pick<H>(wbg[u], ri)), racc);
                     }
                 }
             }
@@ -920,7 +975,8 @@ template <int K>
 eeg_status launch_solve(eeg_ppr* p, SolveArgs& a, uint32_t bps, cudaStream_t st) {
     const uint64_t work = std::max<uint64_t>(a.g.nchunks, ((uint64_t)a.n * 16 + 31) / 32);
     if (p->W == 1) return launch_coop(k_ppr_scalar<K>, &a, p->vg->device, bps, work, st);
-    return launch_coop(k_ppr_rows<K>, &a, p->vg->device, bps, work, st);
+    if (p->W == 32) return launch_coop(k_ppr_rows<K, 8>, &a, p->vg->device, bps, work, st);
+    return launch_coop(k_ppr_rows<K, 16>, &a, p->vg->device, bps, work, st);
 }
 
 template <int K>
@@ -931,8 +987,10 @@ eeg_status launch_grad(eeg_ppr* p, GradArgs& a, cudaStream_t st) {
     const unsigned blocks = (unsigned)((warps * 32 + PPR_TPB - 1) / PPR_TPB);
     if (p->W == 1)
         k_ppr_grad_scalar<K><<<blocks, PPR_TPB, 0, st>>>(a);
+    else if (p->W == 32)
+        k_ppr_grad_rows<K, 8><<<blocks, PPR_TPB, 0, st>>>(a);
     else
-        k_ppr_grad_rows<K><<<blocks, PPR_TPB, 0, st>>>(a);
+        k_ppr_grad_rows<K, 16><<<blocks, PPR_TPB, 0, st>>>(a);
     EEG_CUDA(cudaGetLastError());
     return EEG_OK;
 }
@@ -1041,7 +1099,7 @@ EEG_API eeg_status eeg_ppr_create(eeg_vgraph* vg, uint32_t columns, eeg_ppr** ou
     eeg_ppr* p = new eeg_ppr();
     p->vg = vg;
     p->C = columns;
-    p->W = columns == 1 ? 1u : PPR_W;
+    p->W = columns == 1 ? 1u : (columns <= 32 ? 32u : PPR_W);  // row width: 128-B rows up to 32 columns
     const size_t n = vg->n, rows = n * p->W;
     eeg_status s = EEG_OK;
     auto run = [&]() -> eeg_status {

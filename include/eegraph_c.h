@@ -324,7 +324,8 @@ EEG_API eeg_status eeg_run_noalloc(eeg_algo algo, eeg_variant variant, uint32_t 
  * graph, the adjoint over the forward graph (no atomics, no transpose at run time, no iterate storage).
  * FP32 values and accumulation; the stop test d/(1-d)*||Y_{k+1}-Y_k||_1 <= tol*||Y_{k+1}||_1 (all columns
  * together, eeg_options.pr_tolerance, default 1e-7) is reduced in FP64. C = 1 runs the single-column
- * kernels (the plain form); 2 <= C <= 64 runs the batched row kernels (rows padded to 64 columns). */
+ * kernels (the plain form); 2 <= C <= 64 runs the batched row kernels (rows padded to 32 columns for
+ * C <= 32, else to 64). */
 typedef struct eeg_ppr eeg_ppr;
 /* vg must be built with EEG_VG_REVERSE | EEG_VG_EDGE_IDS and outlive the handle. */
 EEG_API eeg_status eeg_ppr_create(eeg_vgraph* vg, uint32_t columns, eeg_ppr** out);

@@ -52,7 +52,7 @@ def _rel_l1(a, b):
 
 
 @pytest.mark.parametrize("K", [4, 8, 16])
-@pytest.mark.parametrize("C", [1, 5, 64])
+@pytest.mark.parametrize("C", [1, 5, 32, 33, 64])  # plain form; 128-B rows (<= 32 columns); 256-B rows
 def test_ppr_matches_fp64_oracle(gpu, K, C):
     E = gpu
     n, s, d, w, vg = _graph(E, 11, 16, seed=K + C, K=K)
@@ -82,7 +82,7 @@ def test_ppr_hubs_span_groups(gpu):
     for K in (4, 8, 16):
         n, s, d, w, vg = _graph(E, 14, 4, seed=3, K=K, extra=extra)
         rng = np.random.default_rng(K)
-        for C in (1, 64):
+        for C in (1, 20, 64):
             T = _teleport(n, C, 32, rng)
             T[0, :] += 0.5
             G = rng.standard_normal((n, C)).astype(np.float32)
@@ -252,4 +252,33 @@ def test_ppr_errors(gpu):
         # a directed ring: x_{i+1} = d x_i, x_0 = (1-d) + d x_{n-1}
         ref = oracle.ppr_solve(n, s, d, np.ones(n), T, damping=D)[0]
         assert _nl1(X, ref) <= 1e-6
+    vg.close()
+
+
+def test_ppr_column_shards_sum_to_batch(gpu):
+    """Column sharding (one shard per GPU): each shard is an independent solve over its columns, and the
+    edge gradients of the whole batch are the sum of the shards' (the loss is a sum over columns)."""
+    E = gpu
+    n, s, d, w, vg = _graph(E, 12, 16, seed=21, K=8)
+    rng = np.random.default_rng(21)
+    C = 64
+    T = _teleport(n, C, 32, rng)
+    G = rng.standard_normal((n, C)).astype(np.float32)
+    with E.PPR(vg, C) as p:
+        p.set_weights(w)
+        X, _ = p.forward(T)
+        full, _ = p.adjoint(G)
+    for world in (2, 3):
+        cols = E.shard_columns(C, world)
+        assert sorted(c for sh in cols for c in sh) == list(range(C))
+        dw = np.zeros_like(full["dw"], dtype=np.float64)
+        for sh in cols:
+            with E.PPR(vg, len(sh)) as p:
+                p.set_weights(w)
+                Xs, _ = p.forward(np.ascontiguousarray(T[:, sh]))
+                out, _ = p.adjoint(np.ascontiguousarray(G[:, sh]))
+            assert _nl1(Xs, X[:, sh]) <= 2e-6
+            assert _nl1(out["dt"], full["dt"][:, sh]) <= 2e-6
+            dw += out["dw"]
+        assert _rel_l1(dw, full["dw"]) <= 1e-5, (world, _rel_l1(dw, full["dw"]))
     vg.close()

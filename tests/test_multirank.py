@@ -103,3 +103,15 @@ def test_shards_across_two_ranks():
         flat = sorted(i for sh in got for i in sh)
         assert flat == list(range(300))  # disjoint cover, agreed without exchanging the partition
         assert ms == 6.0 and nq == 300.0
+
+
+def test_shard_columns():
+    import eegraph_gb300 as E
+
+    for C in (1, 2, 31, 64):
+        for world in (1, 2, 3, 4, 8):
+            sh = E.shard_columns(C, world)
+            assert len(sh) == world
+            assert [c for s in sh for c in s] == list(range(C))  # contiguous, in order
+            sizes = [len(s) for s in sh]
+            assert max(sizes) - min(sizes) <= 1
