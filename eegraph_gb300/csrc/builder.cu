@@ -149,11 +149,11 @@ constexpr int R_TILE = R_TPB * R_ITEMS;
 constexpr int R_BINS = 256;
 static_assert(R_TPB == R_BINS, "one thread per digit in the cross-warp prefix");
 
-// 0-based owner/neighbour (+ weight, or the input edge index when eid != 0) into the sort buffers;
-// endpoints outside [0, n) raise err.
+// 0-based owner/neighbour (+ weight, or the arc index when eid != 0) of the m input edges into the sort
+// buffers; with sym, arc m + e is the reverse of edge e. Endpoints outside [0, n) raise err.
 __global__ void k_prepare(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, const uint32_t* __restrict__ w,
                           uint64_t m, uint32_t n, uint32_t shift, uint32_t* __restrict__ key, uint32_t* __restrict__ nb,
-                          uint32_t* __restrict__ wt, uint32_t* __restrict__ err, int eid) {
+                          uint32_t* __restrict__ wt, uint32_t* __restrict__ err, int eid, int sym) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t s = a[e] - shift, t = b[e] - shift;
         if (s >= n || t >= n) {
@@ -161,14 +161,21 @@ __global__ void k_prepare(const uint32_t* __restrict__ a, const uint32_t* __rest
             s = 0;
             t = 0;
         }
+        const uint32_t wv = w ? w[e] : 1u;
         key[e] = s;
         nb[e] = t;
-        if (wt) wt[e] = eid ? (uint32_t)e : (w ? w[e] : 1u);
+        if (wt) wt[e] = eid ? (uint32_t)e : wv;
+        if (sym) {
+            key[m + e] = t;
+            nb[m + e] = s;
+            if (wt) wt[m + e] = eid ? (uint32_t)(m + e) : wv;
+        }
     }
 }
 
-// Same, four edges per thread with 128-bit loads and stores (all arrays 16-byte aligned): when the
-// inputs are page-locked host memory read in place, four times the bytes are in flight per load.
+// Same, four edges per thread with 128-bit loads and stores (all arrays 16-byte aligned, and m a
+// multiple of 4 with sym): when the inputs are page-locked host memory read in place, four times the
+// bytes are in flight per load.
 __device__ __forceinline__ void prep_one(uint32_t s, uint32_t t, uint32_t n, uint32_t shift, uint32_t& ks, uint32_t& kt,
                                          uint32_t* err) {
     s -= shift;
@@ -183,7 +190,7 @@ __device__ __forceinline__ void prep_one(uint32_t s, uint32_t t, uint32_t n, uin
 }
 __global__ void k_prepare4(const uint4* __restrict__ a, const uint4* __restrict__ b, const uint4* __restrict__ w,
                            uint64_t m, uint32_t n, uint32_t shift, uint4* __restrict__ key, uint4* __restrict__ nb,
-                           uint4* __restrict__ wt, uint32_t* __restrict__ err, int eid) {
+                           uint4* __restrict__ wt, uint32_t* __restrict__ err, int eid, int sym) {
     const uint64_t m4 = m / 4, stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m4; i += stride) {
         const uint4 s4 = a[i], t4 = b[i];
@@ -200,6 +207,14 @@ __global__ void k_prepare4(const uint4* __restrict__ a, const uint4* __restrict_
             const uint32_t e = (uint32_t)(4 * i);
             wt[i] = eid ? make_uint4(e, e + 1u, e + 2u, e + 3u) : w4;
         }
+        if (sym) {
+            key[m4 + i] = c;
+            nb[m4 + i] = k;
+            if (wt) {
+                const uint32_t e = (uint32_t)(m + 4 * i);
+                wt[m4 + i] = eid ? make_uint4(e, e + 1u, e + 2u, e + 3u) : w4;
+            }
+        }
     }
     // tail (m % 4 edges)
     const uint32_t* a1 = reinterpret_cast<const uint32_t*>(a);
@@ -211,6 +226,11 @@ __global__ void k_prepare4(const uint4* __restrict__ a, const uint4* __restrict_
         reinterpret_cast<uint32_t*>(key)[e] = ks;
         reinterpret_cast<uint32_t*>(nb)[e] = kt;
         if (wt) reinterpret_cast<uint32_t*>(wt)[e] = eid ? (uint32_t)e : (w1 ? w1[e] : 1u);
+        if (sym) {  // not reached: sym takes this kernel only when m is a multiple of 4
+            reinterpret_cast<uint32_t*>(key)[m + e] = kt;
+            reinterpret_cast<uint32_t*>(nb)[m + e] = ks;
+            if (wt) reinterpret_cast<uint32_t*>(wt)[m + e] = eid ? (uint32_t)(m + e) : (w1 ? w1[e] : 1u);
+        }
     }
 }
 
@@ -353,12 +373,13 @@ __global__ void k_heads(const uint32_t* __restrict__ vstart, uint32_t n, uint32_
 }
 
 // sorted edge i of owner o (rank r = i - rs[o]) goes to slot vstart[o]*K + r: part r/K, lane r%K
-// With veid (edge-index mode) the sorted payload is the input edge index: the weight is gathered from
-// the input array by it and the index is kept per slot.
+// With veid (edge-index mode) the sorted payload is the arc index: the weight is gathered from the
+// input array by it (arc e >= m_in of a symmetrised build is the reverse of input edge e - m_in; m_in
+// is 0 otherwise) and the index is kept per slot.
 __global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __restrict__ nb, const uint32_t* __restrict__ wt,
                         uint64_t m, uint32_t K, const uint32_t* __restrict__ rs, const uint32_t* __restrict__ vstart,
                         uint32_t* __restrict__ vcol, uint32_t* __restrict__ vw, const uint32_t* __restrict__ w_in,
-                        uint32_t* __restrict__ veid) {
+                        uint32_t* __restrict__ veid, uint64_t m_in) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t o = key[i];
         const size_t slot = (size_t)vstart[o] * K + (i - rs[o]);
@@ -366,7 +387,7 @@ __global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __rest
         if (veid) {
             const uint32_t e = wt[i];
             veid[slot] = e;
-            if (vw) vw[slot] = w_in ? w_in[e] : 1u;
+            if (vw) vw[slot] = w_in ? w_in[(m_in && e >= m_in) ? e - m_in : e] : 1u;
         } else if (vw) {
             vw[slot] = wt ? wt[i] : 1u;
         }
@@ -414,11 +435,14 @@ struct TempSet {
 
 // Build one direction. reverse: edges (s,t) are inserted as (t,s) -- the transposed graph.
 // Edges are sorted by owner with a stable radix sort, so each vertex's edges keep the input order
-// (the order the reference's MakeGraph gives them) and the layout is deterministic.
+// (the order the reference's MakeGraph gives them) and the layout is deterministic. With
+// EEG_VG_SYMMETRIZE the vg->m arcs are the vg->m / 2 input edges followed by their reverses.
 eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst,
                            const uint32_t* d_w, bool reverse, cudaStream_t st) {
     const uint32_t n = vg->n, K = vg->K;
     const uint64_t m = vg->m;
+    const bool sym = (vg->flags & EEG_VG_SYMMETRIZE) != 0;
+    const uint64_t m_in = sym ? m / 2 : m;  // input edges
     const uint32_t shift = (vg->flags & EEG_VG_SHIFT_ONE) ? 1u : 0u;
     const uint32_t* a = reverse ? d_dst : d_src;
     const uint32_t* b = reverse ? d_src : d_dst;
@@ -453,14 +477,15 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
     if (m > 0) {
         const uint32_t* wi = with_w ? d_w : nullptr;
         auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
-        if (al16(a) && al16(b) && al16(wi) && m >= 4)
-            k_prepare4<<<grid_for(m / 4, vg->device), B_TPB, 0, st>>>(
+        if (al16(a) && al16(b) && al16(wi) && m_in >= 4 && (!sym || m_in % 4 == 0))
+            k_prepare4<<<grid_for(m_in / 4, vg->device), B_TPB, 0, st>>>(
                 reinterpret_cast<const uint4*>(a), reinterpret_cast<const uint4*>(b), reinterpret_cast<const uint4*>(wi),
-                m, n, shift, reinterpret_cast<uint4*>(key[0]), reinterpret_cast<uint4*>(nb[0]),
-                payload ? reinterpret_cast<uint4*>(wt[0]) : nullptr, err, eid ? 1 : 0);
+                m_in, n, shift, reinterpret_cast<uint4*>(key[0]), reinterpret_cast<uint4*>(nb[0]),
+                payload ? reinterpret_cast<uint4*>(wt[0]) : nullptr, err, eid ? 1 : 0, sym ? 1 : 0);
         else
-            k_prepare<<<grid_for(m, vg->device), B_TPB, 0, st>>>(a, b, wi, m, n, shift, key[0], nb[0],
-                                                                  payload ? wt[0] : nullptr, err, eid ? 1 : 0);
+            k_prepare<<<grid_for(m_in, vg->device), B_TPB, 0, st>>>(a, b, wi, m_in, n, shift, key[0], nb[0],
+                                                                     payload ? wt[0] : nullptr, err, eid ? 1 : 0,
+                                                                     sym ? 1 : 0);
         const uint32_t bits = n > 1 ? 32u - (uint32_t)__builtin_clz(n - 1) : 1u;
         for (uint32_t sh = 0; sh < bits; sh += 8) {
             k_radix_hist<<<(unsigned)ntiles, R_TPB, 0, st>>>(key[cur], m, sh, hist, (uint32_t)ntiles);
@@ -508,7 +533,7 @@ eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const
         EEG_TRY(device_scan_u32(d->vowner, d->vowner, P, true, SCAN_MAX, tmp2, st));
         k_place<<<grid_for(m, vg->device), B_TPB, 0, st>>>(key[cur], nb[cur], payload ? wt[cur] : nullptr, m, K, rs,
                                                             d->vstart, d->vcol, d->vw, with_w ? d_w : nullptr,
-                                                            d->veid);
+                                                            d->veid, sym ? m_in : 0);
     }
     EEG_CUDA(cudaGetLastError());
     vg->bytes += sizeof(uint32_t) * ((size_t)(n + 1) * 2 + (size_t)P + slots * (1 + (with_w ? 1 : 0) + (eid ? 1 : 0)));

@@ -188,7 +188,8 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         set_last_error("null edge arrays");
         return EEG_ERR_INVALID;
     }
-    if (m >= 0xFFFFFFFFull || n == 0xFFFFFFFFu) {
+    const bool symmetrize = (flags & EEG_VG_SYMMETRIZE) != 0;
+    if (m >= (symmetrize ? 0x7FFFFFFFull : 0xFFFFFFFFull) || n == 0xFFFFFFFFu) {
         set_last_error("graph too large for 32-bit ids/offsets");
         return EEG_ERR_UNSUPPORTED;
     }
@@ -200,7 +201,7 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
     eeg_vgraph* vg = new eeg_vgraph();
     cudaGetDevice(&vg->device);
     vg->n = n;
-    vg->m = m;
+    vg->m = symmetrize ? 2 * m : m;  // arcs
     vg->K = K;
     vg->flags = flags;
     vg->managed = (flags & EEG_VG_MANAGED) != 0;
@@ -264,7 +265,7 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         dw = w ? tmp + 2 * m : nullptr;
     }
     s = build_direction(vg, &vg->fwd, ds, dd, dw, false, st);
-    if (s == EEG_OK && !(flags & EEG_VG_REVERSE) && (flags & EEG_VG_SYMMETRIC)) {
+    if (s == EEG_OK && !(flags & EEG_VG_REVERSE) && (flags & (EEG_VG_SYMMETRIC | EEG_VG_SYMMETRIZE))) {
         vg->rev = vg->fwd;  // undirected: in-edges are the out-edges
         vg->has_rev = true;
         vg->rev_alias = true;

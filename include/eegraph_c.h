@@ -152,10 +152,16 @@ enum {
     EEG_VG_SHIFT_ONE = 1u << 3, /* subtract 1 from every id while building (1-based input) */
     EEG_VG_EDGE_IDS = 1u << 4,  /* keep each slot's input edge index (per-edge results in input order;
                                    needed by eeg_ppr_create) */
-    EEG_VG_SYMMETRIC = 1u << 5  /* the caller guarantees an undirected edge list (every arc's reverse is
+    EEG_VG_SYMMETRIC = 1u << 5, /* the caller guarantees an undirected edge list (every arc's reverse is
                                    present with the same weight): the forward graph doubles as the
                                    transposed one, so PageRank runs without a second build. Ignored with
                                    REVERSE; not usable by eeg_ppr_create (needs the transposed edge ids). */
+    EEG_VG_SYMMETRIZE = 1u << 6 /* insert every input edge in both directions: the arcs are the input
+                                   followed by its reverse, as eeg_symmetrize lays them out (so the graph
+                                   is the one built from eeg_symmetrize's output), without that host-side
+                                   copy. Implies EEG_VG_SYMMETRIC. num_edges counts input edges; the graph
+                                   has twice as many arcs, and with EEG_VG_EDGE_IDS the reverse of input
+                                   edge e has index num_edges + e. */
 };
 
 typedef struct eeg_vgraph_info {

@@ -60,3 +60,38 @@ def test_pagerank_on_symmetric_graph_equals_transposed_build(gpu):
     with E.VirtualGraph.build(n, ss, ds, ws, K=8, symmetric=True, edge_ids=True) as c:
         with pytest.raises(E.EEGError):
             E.PPR(c, 4)
+
+
+@pytest.mark.parametrize("K", [4, 8, 16])
+def test_symmetrize_on_device_equals_host_symmetrised_build(gpu, K):
+    """EEG_VG_SYMMETRIZE builds, from the directed list, the virtual graph of symmetrize()'s output
+    (same parts, slots and weights), from host or device arrays, with m a multiple of 4 (128-bit
+    first pass) or not; CC on it gives the oracle's labels."""
+    import torch
+
+    E = gpu
+    for m_extra in (0, 3):
+        s, d, w = E.gen_rmat(12, 8, seed=44 + K, wmin=1, wmax=63)
+        s, d, w = s[: s.size - m_extra], d[: d.size - m_extra], w[: w.size - m_extra]
+        n = 1 << 12
+        ss, ds, ws = E.symmetrize(s, d, w)
+        for weighted in (True, False):
+            wi, wsi = (w, ws) if weighted else (None, None)
+            with E.VirtualGraph.build(n, ss, ds, wsi, K=K, symmetric=True) as ref, \
+                    E.VirtualGraph.build(n, s, d, wi, K=K, symmetrize=True) as got:
+                a, b = ref.download(), got.download()
+                for key in a:
+                    assert np.array_equal(a[key], b[key]), (K, m_extra, weighted, key)
+                assert got.info()["num_edges"] == ss.size
+                assert got.info()["num_rparts"] == got.info()["num_parts"]
+                src = int(np.bincount(ss, minlength=n).argmax())
+                lab, _ = got.run("cc", "async_push_dd", src)
+                assert np.array_equal(lab, oracle.cc_labels(n, ss, ds, wsi if weighted else np.ones_like(ss)))
+        dev = torch.device("cuda")
+        ts, td, tw = (torch.from_numpy(np.ascontiguousarray(x).astype(np.int32)).to(dev) for x in (s, d, w))
+        with E.VirtualGraph.build_device(n, s.size, ts.data_ptr(), td.data_ptr(), tw.data_ptr(), K=K,
+                                         symmetrize=True) as gd, \
+                E.VirtualGraph.build(n, ss, ds, ws, K=K, symmetric=True) as ref:
+            a, b = ref.download(), gd.download()
+            for key in a:
+                assert np.array_equal(a[key], b[key]), (K, m_extra, "device", key)
