@@ -175,30 +175,49 @@ __device__ __noinline__ uint32_t run_query(const BArgs& a, const BGraph& g, cons
             uint32_t cd[K];
 #pragma unroll
             for (int i = 0; i < K; ++i) cd[i] = (valid && col[i] != NO_EDGE) ? __ldcg(&dist[col[i]]) : 0u;
+            // the atomics of a group of slots go out before any of their results is used; a won claim
+            // on the round stamp means the target improved in this round (by this lane or after its
+            // filter read), so the winner appends it (the single-query kernel's rule)
+            constexpr int ATB = K < trav::atomic_group<OP>() ? K : trav::atomic_group<OP>();
 #pragma unroll
-            for (int i = 0; i < K; ++i) {
-                bool claim = false;
-                uint32_t t = 0;
-                if (active && col[i] != NO_EDGE) {
-                    t = col[i];
-                    const uint32_t nd = trav::relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                    if (trav::better<OP>(nd, cd[i])) {
-                        const uint32_t prev = trav::atomic_improve<OP>(&dist[t], nd);
-                        if (trav::better<OP>(nd, prev)) {
-                            if (OP == OP_BFS) claim = true;  // atomicMin admits one first improvement
-                            else claim = __ldcg(&stamp[t]) != tag && atomicExch(&stamp[t], tag) != tag;
+            for (int i0 = 0; i0 < K; i0 += ATB) {
+                uint32_t prev[ATB], ex[ATB];
+                uint32_t hit = 0;
+#pragma unroll
+                for (int j = 0; j < ATB; ++j) {
+                    const int i = i0 + j;
+                    prev[j] = 0u;
+                    ex[j] = tag;
+                    if (active && col[i] != NO_EDGE) {
+                        const uint32_t nd = trav::relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
+                        if (trav::better<OP>(nd, cd[i])) {
+                            hit |= 1u << j;
+                            prev[j] = trav::atomic_improve<OP>(&dist[col[i]], nd);
+                            if (OP != OP_BFS) ex[j] = atomicExch(&stamp[col[i]], tag);
                         }
                     }
                 }
-                const uint32_t mask = __ballot_sync(0xffffffffu, claim);
-                if (mask) {
-                    const uint32_t c = __popc(mask);
-                    if (wcnt + c > (uint32_t)trav::WCAP) {
-                        trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane, g.P);
-                        wcnt = 0;
+#pragma unroll
+                for (int j = 0; j < ATB; ++j) {
+                    const int i = i0 + j;
+                    bool claim = false;
+                    const uint32_t t = col[i];
+                    if ((hit >> j) & 1u) {
+                        if (OP == OP_BFS)  // atomicMin admits one first improvement
+                            claim = trav::better<OP>(trav::relax_value<OP>(d, 1u), prev[j]);
+                        else
+                            claim = ex[j] != tag;
                     }
-                    if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
-                    wcnt += c;
+                    const uint32_t mask = __ballot_sync(0xffffffffu, claim);
+                    if (mask) {
+                        const uint32_t c = __popc(mask);
+                        if (wcnt + c > (uint32_t)trav::WCAP) {
+                            trav::warp_append(g.vstart, &ctrl->qparts[nxt], nullptr, wbuf, wcnt, qnext, lane, g.P);
+                            wcnt = 0;
+                        }
+                        if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
+                        wcnt += c;
+                    }
                 }
             }
         }

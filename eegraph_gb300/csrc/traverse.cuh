@@ -71,6 +71,15 @@ __device__ __forceinline__ bool unreached(uint32_t d) {
     if (OP == OP_SSWP) return d == 0u;
     return false;
 }
+// Slots whose atomics are issued together (value atomic + claim, 2 returned values each): the most that
+// fits the 64-register budget without slowing the kernel -- measured on R-MAT s22 with K = 8, groups of
+// 4 for BFS and SSSP (0.39 / 0.75 ms; 2: 0.40 / 0.77), 2 for SSWP and CC (0.73 / 1.30 ms; 4 spilled
+// registers: 0.80 / 1.50; 1: 0.76 / 1.34).
+template <int OP>
+__host__ __device__ constexpr int atomic_group() {
+    return (OP == OP_SSWP || OP == OP_CC) ? 2 : 4;
+}
+
 template <int OP>
 __device__ __forceinline__ uint32_t relax_value(uint32_t d, uint32_t w) {
     if (OP == OP_BFS) return d + 1u;
@@ -377,41 +386,69 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             const bool fetch = dense ? active : valid;
 #pragma unroll
             for (int i = 0; i < K; ++i) cd[i] = (fetch && col[i] != NO_EDGE) ? a.dist[col[i]] : 0u;
+            // The atomics of ATB slots go out before any of their results is used: for each slot whose
+            // filter read says the target improves, the value atomic and (DD, except BFS levels) the
+            // claim on the target's round stamp are issued together. A won claim means the target
+            // improved in this round -- by this lane, or by another after this lane's filter read (that
+            // read is no older than the round's start, and values move one way only) -- so the winner
+            // appends the target, whoever improved it, and a target improved in a round is appended
+            // exactly once.
+            constexpr int ATB = K < atomic_group<OP>() ? K : atomic_group<OP>();
 #pragma unroll
-            for (int i = 0; i < K; ++i) {
-                bool claim = false;
-                uint32_t t = 0;
-                if (active && col[i] != NO_EDGE) {
-                    t = col[i];
-                    ++my_edges;
-                    const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
-                    if (better<OP>(nd, cd[i])) {
-                        const uint32_t prev = atomic_improve<OP>(&a.dist[t], nd);
-                        if (better<OP>(nd, prev)) {
-                            ++my_updates;
-                            if (TD) changed = 1u;
-                            else if (bfs_levels) claim = true;  // atomicMin admits one first improvement
-                            else claim = atomicExch(&a.stamp[t], tag) != tag;
-                            if (BK && claim) {
-                                const uint32_t key = OP == OP_SSWP ? INF - nd : nd;
-                                if (key >= T) {  // not in this bucket: wait in the far pile
-                                    to_far(t, key);
-                                    claim = false;
-                                }
-                            }
+            for (int i0 = 0; i0 < K; i0 += ATB) {
+                uint32_t prev[ATB], ex[ATB];
+                uint32_t hit = 0;  // slots whose filter passed
+#pragma unroll
+                for (int j = 0; j < ATB; ++j) {
+                    const int i = i0 + j;
+                    prev[j] = 0u;
+                    ex[j] = tag;
+                    if (active && col[i] != NO_EDGE) {
+                        ++my_edges;
+                        const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
+                        if (better<OP>(nd, cd[i])) {
+                            hit |= 1u << j;
+                            prev[j] = atomic_improve<OP>(&a.dist[col[i]], nd);
+                            if (!TD && !bfs_levels) ex[j] = atomicExch(&a.stamp[col[i]], tag);
                         }
                     }
                 }
-                if (!TD) {
-                    const uint32_t mask = __ballot_sync(0xffffffffu, claim);
-                    if (mask) {
-                        const uint32_t c = __popc(mask);
-                        if (wcnt + c > (uint32_t)WCAP) {
-                            warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
-                            wcnt = 0;
+#pragma unroll
+                for (int j = 0; j < ATB; ++j) {
+                    const int i = i0 + j;
+                    bool claim = false;
+                    const uint32_t t = col[i];
+                    if ((hit >> j) & 1u) {
+                        const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
+                        const bool imp = better<OP>(nd, prev[j]);
+                        if (imp) ++my_updates;
+                        if (TD) {
+                            if (imp) changed = 1u;
+                        } else if (bfs_levels) {
+                            claim = imp;  // atomicMin admits one first improvement
+                        } else {
+                            claim = ex[j] != tag;
                         }
-                        if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
-                        wcnt += c;
+                        if (BK && claim) {
+                            const uint32_t now = imp ? nd : prev[j];  // the target's value after this atomic
+                            const uint32_t key = OP == OP_SSWP ? INF - now : now;
+                            if (key >= T) {  // not in this bucket: wait in the far pile
+                                to_far(t, key);
+                                claim = false;
+                            }
+                        }
+                    }
+                    if (!TD) {
+                        const uint32_t mask = __ballot_sync(0xffffffffu, claim);
+                        if (mask) {
+                            const uint32_t c = __popc(mask);
+                            if (wcnt + c > (uint32_t)WCAP) {
+                                warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
+                                wcnt = 0;
+                            }
+                            if (claim) wbuf[wcnt + __popc(mask & lanemask_lt)] = t;
+                            wcnt += c;
+                        }
                     }
                 }
             }
