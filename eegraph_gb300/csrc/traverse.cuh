@@ -289,13 +289,27 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
         }
         const uint32_t* pile_src = BK ? a.fpile + (size_t)fc * a.n : nullptr;
         uint32_t* pile_dst = BK ? a.fpile + (size_t)fdst * a.n : nullptr;
-        auto to_far = [&](uint32_t t, uint32_t key) {
-            if (atomicExch(&a.fflag[t], 1u) != 1u) {
-                const uint32_t pos = atomicAdd(&ctrl->fcnt[fdst], 1u);
+        // Warp-collective: the lanes with `fl` send vertex t (key `key`) to the far pile. A vertex enters
+        // the pile once (its flag); the pile's count and smallest key take one atomic per warp, not per
+        // vertex (same-address atomics from every warp queue at one L2 slice).
+        auto to_far = [&](bool fl, uint32_t t, uint32_t key) {
+            const uint32_t fmask = __ballot_sync(0xffffffffu, fl);
+            if (!fmask) return;
+            const bool app = fl && atomicExch(&a.fflag[t], 1u) != 1u;
+            const uint32_t amask = __ballot_sync(0xffffffffu, app);
+            const uint32_t kmin = __reduce_min_sync(0xffffffffu, fl ? key : 0xFFFFFFFFu);
+            const uint32_t leader = __ffs(fmask) - 1u;
+            uint32_t base = 0;
+            if (lane == leader) {
+                if (amask) base = atomicAdd(&ctrl->fcnt[fdst], (uint32_t)__popc(amask));
+                atomicMin(&ctrl->fmin[fdst], kmin);
+            }
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (app) {
+                const uint32_t pos = base + (uint32_t)__popc(amask & lanemask_lt);
                 if (pos < a.n) pile_dst[pos] = t;
                 else atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
             }
-            atomicMin(&ctrl->fmin[fdst], key);
         };
         // no __restrict__/const-qualified read-only path here: each queue is rewritten every other round
         const uint32_t* qcur = (it & 1u) ? a.q1 : a.q0;
@@ -334,13 +348,15 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             const uint32_t p = p_next;
             ci_next = draw(p_next);
             if (BK && far_round) {  // far round: p is a far vertex; move it back when below T
-                bool move = false;
+                bool move = false, stay = false;
+                uint32_t key = 0;
                 if (p < a.n && atomicExch(&a.fflag[p], 0u) == 1u) {
                     const uint32_t dv = a.dist[p];
-                    const uint32_t key = OP == OP_SSWP ? INF - dv : dv;
+                    key = OP == OP_SSWP ? INF - dv : dv;
                     if (key < T) move = true;
-                    else to_far(p, key);
+                    else stay = true;
                 }
+                to_far(stay, p, key);
                 const uint32_t mask = __ballot_sync(0xffffffffu, move);
                 if (mask) {
                     const uint32_t c = __popc(mask);
@@ -393,7 +409,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             // read is no older than the round's start, and values move one way only) -- so the winner
             // appends the target, whoever improved it, and a target improved in a round is appended
             // exactly once.
-            constexpr int ATB = K < atomic_group<OP>() ? K : atomic_group<OP>();
+            constexpr int ATG = BK ? 2 : atomic_group<OP>();  // the far-pile path takes registers too
+            constexpr int ATB = K < ATG ? K : ATG;
 #pragma unroll
             for (int i0 = 0; i0 < K; i0 += ATB) {
                 uint32_t prev[ATB], ex[ATB];
@@ -416,7 +433,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
 #pragma unroll
                 for (int j = 0; j < ATB; ++j) {
                     const int i = i0 + j;
-                    bool claim = false;
+                    bool claim = false, far = false;
+                    uint32_t fkey = 0;
                     const uint32_t t = col[i];
                     if ((hit >> j) & 1u) {
                         const uint32_t nd = relax_value<OP>(d, OP == OP_BFS ? 1u : wt[i]);
@@ -433,11 +451,13 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                             const uint32_t now = imp ? nd : prev[j];  // the target's value after this atomic
                             const uint32_t key = OP == OP_SSWP ? INF - now : now;
                             if (key >= T) {  // not in this bucket: wait in the far pile
-                                to_far(t, key);
+                                far = true;
+                                fkey = key;
                                 claim = false;
                             }
                         }
                     }
+                    if (BK) to_far(far, t, fkey);
                     if (!TD) {
                         const uint32_t mask = __ballot_sync(0xffffffffu, claim);
                         if (mask) {
