@@ -57,7 +57,19 @@ struct TravArgs {
     uint32_t delta;        // SSSP/SSWP bucket width (bucketed kernels only)
     uint32_t* fpile;       // 3 x n far piles (bucketed kernels only)
     uint32_t* fflag;       // n far flags (1 = in a pile)
+    uint32_t cc_zero;      // CC: relax with weight 0 (connected components)
 };
+
+// The weights of part p (CC in connected-components mode: zeros, nothing loaded).
+template <int OP, int K>
+__device__ __forceinline__ void load_weights(const TravArgs& a, uint32_t p, uint32_t (&wt)[K], uint64_t pol) {
+    if (OP == OP_CC && a.cc_zero) {
+#pragma unroll
+        for (int i = 0; i < K; ++i) wt[i] = 0u;
+    } else {
+        ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+    }
+}
 
 template <int OP>
 __device__ __forceinline__ uint32_t init_value(uint32_t v, uint32_t src) {
@@ -382,7 +394,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                     const uint32_t v = __ldg(&a.vowner[p]);
                     if (!TD) {  // DD: the part is almost surely live -- fetch its row alongside the owner's value
                         ld_part<K>(a.vcol + (size_t)p * K, col, pol);
-                        if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                        if (OP != OP_BFS) load_weights<OP, K>(a, p, wt, pol);
                     }
                     // plain (L1-cached) value reads: the grid barrier's acquire makes the previous round's
                     // values visible; a value improved later in this round re-enqueues its vertex anyway
@@ -390,7 +402,7 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
                     active = !unreached<OP>(d);
                     if (TD && active) {
                         ld_part<K>(a.vcol + (size_t)p * K, col, pol);
-                        if (OP != OP_BFS) ld_part<K>(a.vw + (size_t)p * K, wt, pol);
+                        if (OP != OP_BFS) load_weights<OP, K>(a, p, wt, pol);
                     }
                 }
                 if (active) ++my_parts;

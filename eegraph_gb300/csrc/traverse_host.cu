@@ -60,7 +60,8 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
         set_last_error("source vertex out of range");
         return EEG_ERR_INVALID;
     }
-    if (op != OP_BFS && !vg->fwd.vw && vg->fwd.P > 0) {
+    const bool cc_zero = op == OP_CC && o.cc_components;
+    if (op != OP_BFS && !cc_zero && !vg->fwd.vw && vg->fwd.P > 0) {
         set_last_error("graph was built without weights");
         return EEG_ERR_INVALID;
     }
@@ -87,6 +88,7 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     a.source = source;
     a.seed_all = seed_all ? 1u : 0u;
     a.partner = (variant == EEG_SYNC_PUSH_TD) ? 1u : 0u;
+    a.cc_zero = cc_zero ? 1u : 0u;
     a.max_iters = o.max_iterations ? o.max_iterations : (vg->n > 0xFFFFFFF0u ? 0xFFFFFFFFu : vg->n + 2u);
     if (bucketed) {
         // far rounds come on top of the frontier rounds (each moves at least one vertex back)

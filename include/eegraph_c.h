@@ -216,7 +216,11 @@ typedef struct eeg_options {
                                  whose distance (SSSP) or INF - width (SSWP) is not below the current
                                  threshold waits until the frontier runs empty (0 = plain rounds). Same
                                  results; far fewer rescans on high-diameter graphs. */
-    uint32_t reserved[5];
+    uint32_t cc_components;   /* CC: 1 = connected components, relaxing with weight 0 instead of the edge
+                                 weight, so label(v) = the smallest id in v's component when every vertex
+                                 is seeded (ASYNC_* and SYNC_PUSH_TD) -- an extension, not the reference's
+                                 min-plus labels (0, the default) */
+    uint32_t reserved[4];
 } eeg_options;
 
 typedef struct eeg_result {

@@ -95,3 +95,40 @@ def test_symmetrize_on_device_equals_host_symmetrised_build(gpu, K):
             a, b = ref.download(), gd.download()
             for key in a:
                 assert np.array_equal(a[key], b[key]), (K, m_extra, "device", key)
+
+
+def _component_minima(n, s, d):
+    """Smallest vertex id of each vertex's connected component (scipy, an independent check)."""
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    g = sp.coo_matrix((np.ones(s.size), (s.astype(np.int64), d.astype(np.int64))), shape=(n, n))
+    _, comp = csgraph.connected_components(g, directed=False)
+    first = np.full(comp.max() + 1, n, np.int64)
+    np.minimum.at(first, comp, np.arange(n))
+    return first[comp].astype(np.uint32)
+
+
+@pytest.mark.parametrize("K", [4, 8, 16])
+def test_cc_components_mode(gpu, K):
+    """eeg_options.cc_components: CC relaxes with weight 0, so every all-seeded variant labels each vertex
+    with the smallest id of its component (scipy's components); SYNC_PUSH_DD keeps its source-seeded
+    fixed point (the oracle with zero weights). Weights are neither needed nor read."""
+    E = gpu
+    rng = np.random.default_rng(K)
+    n = 6000
+    s = rng.integers(0, n, 2500).astype(np.uint32)  # sparse: many components, many isolated vertices
+    d = rng.integers(0, n, 2500).astype(np.uint32)
+    graphs = [("sparse", n, *E.symmetrize(s, d, None)[:2])]
+    for name, gn, gs, gd, gw in _sym_graphs(E):
+        graphs.append((name, gn, gs, gd))
+    for name, gn, gs, gd in graphs:
+        want = _component_minima(gn, gs, gd)
+        zeros = np.zeros(gs.size, np.uint32)
+        src = int(np.bincount(gs, minlength=gn).argmax())
+        with E.VirtualGraph.build(gn, gs, gd, None, K=K, symmetric=True) as vg:
+            for variant in VARIANTS:
+                got, _ = vg.run("cc", variant, src, cc_components=True)
+                if variant == "sync_push_dd":
+                    assert np.array_equal(got, oracle.expected("cc", variant, gn, gs, gd, zeros, src)), (name, K)
+                else:
+                    assert np.array_equal(got, want), (name, variant, K)
