@@ -268,7 +268,8 @@ def bench_gpu(args) -> None:
         g1 = E.VirtualGraph.build_device(n, m, ptr["s"], ptr["d"], ptr["w"], K=args.k, stream=stream)
         g2 = E.VirtualGraph.build_device(n, m, ptr["s"], ptr["d"], ptr["w"], K=args.k, symmetrize=True,
                                          stream=stream)
-        g3 = E.VirtualGraph.build_device(n, m, ptr["s"], ptr["d"], None, K=args.pr_k, reverse=True, stream=stream)
+        g3 = E.VirtualGraph.build_device(n, m, ptr["s"], ptr["d"], None, K=args.pr_k, reverse_only=True,
+                                         stream=stream)
         src_e2e = g1.info()["max_degree_vertex"]
         for algo, variant in ALGO_PLAN:
             (g2 if algo == "cc" else (g3 if algo == "pr" else g1)).run(algo, variant, src_e2e, out=host_out[algo],

@@ -29,7 +29,7 @@ VARIANTS = {"async_push_td": ASYNC_PUSH_TD, "async_push_dd": ASYNC_PUSH_DD,
 ALGOS = {"bfs": BFS, "sssp": SSSP, "sswp": SSWP, "cc": CC, "pr": PR}
 DIST_INFINITY = 4294967294
 VG_REVERSE, VG_MANAGED, VG_INPUT_DEVICE, VG_SHIFT_ONE, VG_EDGE_IDS, VG_SYMMETRIC = 1, 2, 4, 8, 16, 32
-VG_SYMMETRIZE = 64
+VG_SYMMETRIZE, VG_REVERSE_ONLY = 64, 128
 
 # every function the C header declares (checked by the CPU test suite)
 EXPORTED = [
@@ -277,13 +277,14 @@ class VirtualGraph:
     @classmethod
     def build(cls, num_nodes: int, src, dst, w=None, K: int = 8, reverse: bool = False, managed: bool = False,
               stream: int | None = None, shift_one: bool = False, edge_ids: bool = False,
-              symmetric: bool = False, symmetrize: bool = False) -> "VirtualGraph":
+              symmetric: bool = False, symmetrize: bool = False, reverse_only: bool = False) -> "VirtualGraph":
         """Build from host arrays (copied to the device inside the call). symmetric=True declares an
         undirected edge list (every arc's reverse present with the same weight); symmetrize=True inserts
-        every edge in both directions on the device (the graph of symmetrize(src, dst, w))."""
+        every edge in both directions on the device (the graph of symmetrize(src, dst, w)); reverse_only=True
+        builds only what PageRank reads (the transposed graph and the out-degrees)."""
         flags = (VG_REVERSE if reverse else 0) | (VG_MANAGED if managed else 0) | (VG_SHIFT_ONE if shift_one else 0)
         flags |= (VG_EDGE_IDS if edge_ids else 0) | (VG_SYMMETRIC if symmetric else 0)
-        flags |= VG_SYMMETRIZE if symmetrize else 0
+        flags |= (VG_SYMMETRIZE if symmetrize else 0) | (VG_REVERSE_ONLY if reverse_only else 0)
         h = C.c_void_p()
         src, dst = _u32(src), _u32(dst)
         wi = _u32(w) if w is not None else None
@@ -294,10 +295,11 @@ class VirtualGraph:
     @classmethod
     def build_device(cls, num_nodes: int, num_edges: int, src_ptr: int, dst_ptr: int, w_ptr: int | None, K: int = 8,
                      reverse: bool = False, stream: int | None = None, edge_ids: bool = False,
-                     symmetrize: bool = False) -> "VirtualGraph":
-        """Build from device arrays of num_edges input edges (symmetrize: both directions of each)."""
+                     symmetrize: bool = False, reverse_only: bool = False) -> "VirtualGraph":
+        """Build from device arrays of num_edges input edges (symmetrize: both directions of each;
+        reverse_only: only the transposed graph and the out-degrees, for PageRank)."""
         flags = VG_INPUT_DEVICE | (VG_REVERSE if reverse else 0) | (VG_EDGE_IDS if edge_ids else 0)
-        flags |= VG_SYMMETRIZE if symmetrize else 0
+        flags |= (VG_SYMMETRIZE if symmetrize else 0) | (VG_REVERSE_ONLY if reverse_only else 0)
         h = C.c_void_p()
         _check(_lib.eeg_vgraph_build_arrays(num_nodes, num_edges, C.c_void_p(src_ptr), C.c_void_p(dst_ptr),
                                             C.c_void_p(w_ptr) if w_ptr else None, K, flags,

@@ -459,9 +459,10 @@ EEG_API eeg_status eeg_batch_create(eeg_vgraph* const* graphs, uint32_t num_grap
     std::vector<BGraph> hg(num_graphs);
     for (uint32_t i = 0; i < num_graphs; ++i) {
         eeg_vgraph* vg = graphs[i];
-        if (!vg || vg->device != b->device || (!vg->fwd.vw && vg->fwd.P)) {
+        if (!vg || vg->device != b->device || !vg->fwd_parts || (!vg->fwd.vw && vg->fwd.P)) {
             delete b;
-            set_last_error("eeg_batch_create: graph missing, on another device, or without weights");
+            set_last_error("eeg_batch_create: graph missing, on another device, without weights or without "
+                           "forward parts (EEG_VG_REVERSE_ONLY)");
             return EEG_ERR_INVALID;
         }
         b->graphs.push_back(vg);

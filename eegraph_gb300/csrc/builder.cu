@@ -394,6 +394,28 @@ __global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __rest
     }
 }
 
+// Out-degree histogram of the input edges (with sym, of both directions); endpoints outside [0, n)
+// are counted nowhere (the transposed build reports them).
+__global__ void k_outdeg(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t m, uint32_t n,
+                         uint32_t shift, int sym, uint32_t* __restrict__ deg) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = a[e] - shift, t = b[e] - shift;
+        if (s < n && t < n) {
+            atomicAdd(&deg[s], 1u);
+            if (sym) atomicAdd(&deg[t], 1u);
+        }
+    }
+}
+// Largest degree and its smallest vertex, packed (degree << 32 | ~vertex) into one 64-bit max.
+__global__ void k_deg_best(const uint32_t* __restrict__ deg, uint32_t n, unsigned long long* best) {
+    unsigned long long b = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (deg[v]) b = max(b, ((unsigned long long)deg[v] << 32) | (0xFFFFFFFFu - v));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b = max(b, __shfl_down_sync(0xffffffffu, b, o));
+    if ((threadIdx.x & 31u) == 0 && b) atomicMax(best, b);
+}
+
 }  // namespace
 
 int sm_count(int device) {
@@ -432,6 +454,30 @@ struct TempSet {
     }
 };
 }  // namespace
+
+eeg_status build_out_degrees(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst, cudaStream_t st) {
+    const uint32_t n = vg->n;
+    const bool sym = (vg->flags & EEG_VG_SYMMETRIZE) != 0;
+    const uint64_t m_in = sym ? vg->m / 2 : vg->m;
+    const uint32_t shift = (vg->flags & EEG_VG_SHIFT_ONE) ? 1u : 0u;
+    EEG_TRY(vg_alloc(vg, (void**)&d->deg, sizeof(uint32_t) * (size_t)(n + 1)));
+    TempSet T(st);
+    unsigned long long* best = nullptr;
+    EEG_TRY(T.get((void**)&best, sizeof(unsigned long long)));
+    EEG_CUDA(cudaMemsetAsync(d->deg, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
+    EEG_CUDA(cudaMemsetAsync(best, 0, sizeof(unsigned long long), st));
+    if (m_in) k_outdeg<<<grid_for(m_in, vg->device), B_TPB, 0, st>>>(d_src, d_dst, m_in, n, shift, sym ? 1 : 0, d->deg);
+    k_deg_best<<<grid_for(n, vg->device), B_TPB, 0, st>>>(d->deg, n, best);
+    EEG_CUDA(cudaGetLastError());
+    unsigned long long hb = 0;
+    EEG_CUDA(cudaMemcpyAsync(&hb, best, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    EEG_CUDA(cudaStreamSynchronize(st));
+    vg->max_deg = (uint32_t)(hb >> 32);
+    vg->max_deg_vertex = hb ? 0xFFFFFFFFu - (uint32_t)(hb & 0xFFFFFFFFu) : 0u;
+    d->P = 0;
+    vg->bytes += sizeof(uint32_t) * (size_t)(n + 1);
+    return EEG_OK;
+}
 
 // Build one direction. reverse: edges (s,t) are inserted as (t,s) -- the transposed graph.
 // Edges are sorted by owner with a stable radix sort, so each vertex's edges keep the input order

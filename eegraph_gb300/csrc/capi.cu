@@ -188,6 +188,7 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         set_last_error("null edge arrays");
         return EEG_ERR_INVALID;
     }
+    if (flags & EEG_VG_REVERSE_ONLY) flags |= EEG_VG_REVERSE;
     const bool symmetrize = (flags & EEG_VG_SYMMETRIZE) != 0;
     if (m >= (symmetrize ? 0x7FFFFFFFull : 0xFFFFFFFFull) || n == 0xFFFFFFFFu) {
         set_last_error("graph too large for 32-bit ids/offsets");
@@ -264,7 +265,12 @@ static eeg_status build_impl(uint32_t n, uint64_t m, const uint32_t* src, const 
         dd = tmp + m;
         dw = w ? tmp + 2 * m : nullptr;
     }
-    s = build_direction(vg, &vg->fwd, ds, dd, dw, false, st);
+    if (flags & EEG_VG_REVERSE_ONLY) {
+        s = build_out_degrees(vg, &vg->fwd, ds, dd, st);
+        vg->fwd_parts = false;
+    } else {
+        s = build_direction(vg, &vg->fwd, ds, dd, dw, false, st);
+    }
     if (s == EEG_OK && !(flags & EEG_VG_REVERSE) && (flags & (EEG_VG_SYMMETRIC | EEG_VG_SYMMETRIZE))) {
         vg->rev = vg->fwd;  // undirected: in-edges are the out-edges
         vg->has_rev = true;
@@ -326,6 +332,10 @@ EEG_API eeg_status eeg_vgraph_download(const eeg_vgraph* vg, uint32_t* vstart, u
                                        uint32_t* vw, uint32_t* outdeg) {
     if (!vg) {
         set_last_error("null argument");
+        return EEG_ERR_INVALID;
+    }
+    if (!vg->fwd_parts) {
+        set_last_error("graph built with EEG_VG_REVERSE_ONLY has no forward parts");
         return EEG_ERR_INVALID;
     }
     EEG_CUDA(cudaSetDevice(vg->device));

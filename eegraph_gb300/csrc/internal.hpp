@@ -95,6 +95,7 @@ struct eeg_vgraph {
     eeg::VDir fwd, rev;
     bool has_rev = false;
     bool rev_alias = false;  // EEG_VG_SYMMETRIC: rev shares fwd's arrays
+    bool fwd_parts = true;   // false with EEG_VG_REVERSE_ONLY: fwd holds the out-degrees only
     bool weighted = true;
     uint32_t max_deg = 0, max_deg_vertex = 0;
     uint64_t bytes = 0;
@@ -111,6 +112,8 @@ void vg_free(eeg_vgraph* vg, void* p);
 // builder (builder.cu)
 eeg_status build_direction(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst,
                            const uint32_t* d_w, bool reverse, cudaStream_t st);
+// Out-degrees (and the largest, with its vertex) without building the forward parts.
+eeg_status build_out_degrees(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, const uint32_t* d_dst, cudaStream_t st);
 
 // kernels (traverse.cu / pagerank.cu)
 eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t source, const eeg_options& o,

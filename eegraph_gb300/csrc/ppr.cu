@@ -1087,6 +1087,10 @@ EEG_API eeg_status eeg_ppr_create(eeg_vgraph* vg, uint32_t columns, eeg_ppr** ou
         set_last_error("columns must be in [1, 64]");
         return EEG_ERR_INVALID;
     }
+    if (!vg->fwd_parts) {
+        set_last_error("personalised PageRank needs the forward parts (not EEG_VG_REVERSE_ONLY)");
+        return EEG_ERR_INVALID;
+    }
     if (!vg->has_rev || vg->rev_alias || !(vg->flags & EEG_VG_EDGE_IDS) || !vg->fwd.veid || !vg->rev.veid) {
         set_last_error("personalised PageRank needs a graph built with EEG_VG_REVERSE | EEG_VG_EDGE_IDS");
         return EEG_ERR_INVALID;

@@ -56,6 +56,10 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
         set_last_error("empty graph");
         return EEG_ERR_INVALID;
     }
+    if (!vg->fwd_parts) {
+        set_last_error("graph built with EEG_VG_REVERSE_ONLY has no forward parts (PageRank only)");
+        return EEG_ERR_INVALID;
+    }
     if (source >= vg->n) {
         set_last_error("source vertex out of range");
         return EEG_ERR_INVALID;

@@ -156,12 +156,16 @@ enum {
                                    present with the same weight): the forward graph doubles as the
                                    transposed one, so PageRank runs without a second build. Ignored with
                                    REVERSE; not usable by eeg_ppr_create (needs the transposed edge ids). */
-    EEG_VG_SYMMETRIZE = 1u << 6 /* insert every input edge in both directions: the arcs are the input
+    EEG_VG_SYMMETRIZE = 1u << 6, /* insert every input edge in both directions: the arcs are the input
                                    followed by its reverse, as eeg_symmetrize lays them out (so the graph
                                    is the one built from eeg_symmetrize's output), without that host-side
                                    copy. Implies EEG_VG_SYMMETRIC. num_edges counts input edges; the graph
                                    has twice as many arcs, and with EEG_VG_EDGE_IDS the reverse of input
                                    edge e has index num_edges + e. */
+    EEG_VG_REVERSE_ONLY = 1u << 7 /* build only what PageRank reads: the transposed graph and the
+                                   out-degrees (implies EEG_VG_REVERSE). The forward parts are not
+                                   built, so the traversals, eeg_batch_create, eeg_ppr_create and
+                                   eeg_vgraph_download refuse such a graph (EEG_ERR_INVALID). */
 };
 
 typedef struct eeg_vgraph_info {

@@ -132,3 +132,38 @@ def test_cc_components_mode(gpu, K):
                     assert np.array_equal(got, oracle.expected("cc", variant, gn, gs, gd, zeros, src)), (name, K)
                 else:
                     assert np.array_equal(got, want), (name, variant, K)
+
+
+def test_reverse_only_build(gpu):
+    """EEG_VG_REVERSE_ONLY: the transposed graph and out-degrees only. PageRank on it equals PageRank on a
+    full two-direction build bit for bit (same transposed parts, same degrees), for plain and symmetrised
+    input; everything that needs the forward parts refuses the graph."""
+    import torch
+
+    E = gpu
+    s, d, w = E.gen_rmat(12, 8, seed=47, wmin=1, wmax=63)
+    n = 1 << 12
+    for sym in (False, True):
+        with E.VirtualGraph.build(n, s, d, None, K=8, reverse=True, symmetrize=sym) as full, \
+                E.VirtualGraph.build(n, s, d, None, K=8, reverse_only=True, symmetrize=sym) as ro:
+            fi, ri = full.info(), ro.info()
+            assert ri["num_parts"] == 0 and ri["num_rparts"] == fi["num_rparts"]
+            assert ri["max_out_degree"] == fi["max_out_degree"]
+            assert ri["max_degree_vertex"] == fi["max_degree_vertex"]
+            for variant in ("sync_push_td", "async_push_td"):
+                xa, _ = full.run("pr", variant)
+                xb, _ = ro.run("pr", variant)
+                assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32)), (sym, variant)
+            with pytest.raises(E.EEGError):
+                ro.run("bfs", "sync_push_dd", 0)
+            with pytest.raises(E.EEGError):
+                ro.download()
+            with pytest.raises(E.EEGError):
+                E.Batch([ro])
+    dev = torch.device("cuda")
+    ts, td = (torch.from_numpy(np.ascontiguousarray(x).astype(np.int32)).to(dev) for x in (s, d))
+    with E.VirtualGraph.build_device(n, s.size, ts.data_ptr(), td.data_ptr(), None, K=16, reverse_only=True) as gd, \
+            E.VirtualGraph.build(n, s, d, None, K=16, reverse=True) as ref:
+        xa, _ = gd.run("pr", "sync_push_td")
+        xb, _ = ref.run("pr", "sync_push_td")
+        assert np.array_equal(xa.view(np.uint32), xb.view(np.uint32))
