@@ -41,7 +41,7 @@ EXPORTED = [
     "eeg_vgraph_export_reference_layout", "eeg_vgraph_destroy", "eeg_options_init", "eeg_run",
     "eeg_run_noalloc", "eeg_energy_begin", "eeg_energy_mark", "eeg_energy_end", "eeg_energy_destroy",
     "eeg_batch_create", "eeg_batch_set_queries", "eeg_batch_query_offset", "eeg_batch_run", "eeg_batch_rounds",
-    "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_batch_query_times",
+    "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_autotune", "eeg_batch_query_times",
     "eeg_ppr_create", "eeg_ppr_set_weights", "eeg_ppr_forward", "eeg_ppr_adjoint", "eeg_ppr_destroy",
     "eeg_batch_set_grid_queries", "eeg_batch_get_config",
 ]
@@ -66,6 +66,10 @@ class Options(C.Structure):
                 ("record_activity", C.c_uint32), ("timeout_ms", C.c_uint32), ("host_loop", C.c_uint32),
                 ("pr_hot_limit", C.c_uint32), ("delta", C.c_uint32), ("cc_components", C.c_uint32),
                 ("reserved", C.c_uint32 * 4)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("K", C.c_uint32), ("variant", C.c_int), ("ms", C.c_float), ("ms_table", C.c_float * 12)]
 
 
 class Result(C.Structure):
@@ -134,6 +138,7 @@ def _load() -> C.CDLL:
         "eeg_batch_get_config": (C.c_int, [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
         "eeg_autotune_k": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_uint32, C.POINTER(C.c_uint32),
                                      C.POINTER(C.c_float)]),
+        "eeg_autotune": (C.c_int, [C.c_uint32, C.c_uint64, vp, vp, vp, C.c_int, C.c_uint32, C.POINTER(Tuning)]),
         "eeg_ppr_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
         "eeg_ppr_set_weights": (C.c_int, [vp, vp, C.c_int]),
         "eeg_ppr_forward": (C.c_int, [vp, vp, C.c_int, vp, C.c_int, C.POINTER(Options), vp, C.POINTER(Result)]),
@@ -629,6 +634,19 @@ def autotune_k(num_nodes: int, src, dst, w=None, reps: int = 3):
     ms = (C.c_float * 3)()
     _check(_lib.eeg_autotune_k(num_nodes, src.size, _ptr(src), _ptr(dst), _ptr(wi), reps, C.byref(k), ms), "autotune_k")
     return k.value, {4: ms[0], 8: ms[1], 16: ms[2]}
+
+
+def autotune(num_nodes: int, src, dst, w=None, algo="sssp", reps: int = 3) -> dict:
+    """Fastest (K, variant) for this graph and algorithm among K in {4, 8, 16} and the variants with the
+    default's fixed point; returns {"K", "variant", "ms", "table": {(K, variant): ms}}."""
+    src, dst = _u32(src), _u32(dst)
+    wi = _u32(w) if w is not None else None
+    a = ALGOS[algo] if isinstance(algo, str) else int(algo)
+    t = Tuning()
+    _check(_lib.eeg_autotune(num_nodes, src.size, _ptr(src), _ptr(dst), _ptr(wi), a, reps, C.byref(t)), "autotune")
+    names = {v: k for k, v in VARIANTS.items()}
+    table = {((4, 8, 16)[i // 4], names[i % 4]): t.ms_table[i] for i in range(12) if t.ms_table[i] >= 0}
+    return {"K": t.K, "variant": names[t.variant], "ms": t.ms, "table": table}
 
 
 # ---------------------------------------------------------------- energy

@@ -428,6 +428,49 @@ EEG_API eeg_status eeg_autotune_k(uint32_t num_nodes, uint64_t num_edges, const 
     return EEG_OK;
 }
 
+EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                const uint32_t* weight, eeg_algo algo, uint32_t reps, eeg_tuning* out) {
+    if (!out || (unsigned)algo > (unsigned)EEG_PR) {
+        set_last_error("eeg_autotune: null output or unknown algorithm");
+        return EEG_ERR_INVALID;
+    }
+    reps = reps ? reps : 3;
+    const uint32_t ks[3] = {4, 8, 16};
+    eeg_tuning t{};
+    t.ms = -1.f;
+    for (float& x : t.ms_table) x = -1.f;
+    const uint32_t flags = algo == EEG_PR ? (uint32_t)EEG_VG_REVERSE_ONLY : 0u;
+    const uint32_t* w = (algo == EEG_BFS || algo == EEG_PR) ? nullptr : weight;
+    for (int i = 0; i < 3; ++i) {
+        eeg_vgraph* vg = nullptr;
+        EEG_TRY(eeg_vgraph_build_arrays(num_nodes, num_edges, src, dst, w, ks[i], flags, nullptr, &vg));
+        eeg_status s = EEG_OK;
+        for (int v = 0; v < 4 && s == EEG_OK; ++v) {
+            if (algo == EEG_CC && v == EEG_SYNC_PUSH_DD) continue;  // another fixed point
+            std::vector<float> times;
+            for (uint32_t r = 0; r < reps + 1 && s == EEG_OK; ++r) {  // the first run warms up
+                eeg_result res{};
+                s = eeg_run(vg, algo, (eeg_variant)v, vg->max_deg_vertex, nullptr, nullptr, 0, nullptr, 0, nullptr,
+                            &res);
+                if (s == EEG_OK && r > 0) times.push_back(res.kernel_ms);
+            }
+            if (s != EEG_OK) break;
+            std::sort(times.begin(), times.end());
+            const float med = times[times.size() / 2];
+            t.ms_table[i * 4 + v] = med;
+            if (t.ms < 0.f || med < t.ms) {
+                t.ms = med;
+                t.K = ks[i];
+                t.variant = (eeg_variant)v;
+            }
+        }
+        eeg_vgraph_destroy(vg);
+        if (s != EEG_OK) return s;
+    }
+    *out = t;
+    return EEG_OK;
+}
+
 EEG_API void eeg_vgraph_destroy(eeg_vgraph* vg) {
     if (!vg) return;
     int prev = 0;

@@ -305,6 +305,23 @@ EEG_API void eeg_batch_destroy(eeg_batch* b);
 EEG_API eeg_status eeg_autotune_k(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
                                   const uint32_t* weight, uint32_t reps, uint32_t* best_k, float* ms_per_k);
 
+/* Autotuner per graph and algorithm (no counterpart in the reference): for K in {4, 8, 16} and every
+ * variant whose fixed point equals the default's -- all four for BFS, SSSP, SSWP and PageRank; for CC
+ * all but SYNC_PUSH_DD, whose source-seeded fixed point differs -- build the graph (PageRank: its
+ * transposed graph only), run from the highest-out-degree vertex, one warm-up then `reps` runs, and
+ * keep the median kernel time. ms_table[k_index * 4 + variant] (k_index 0, 1, 2 for K = 4, 8, 16) holds
+ * the medians, -1 where a variant is not tried. The CTA shape is not a knob: the persistent kernels
+ * run the register-limited shape measured best, and hubs are split into K-bounded parts by the builder
+ * rather than handed to warps or CTAs by a degree threshold. Host arrays. */
+typedef struct eeg_tuning {
+    uint32_t K;
+    eeg_variant variant;
+    float ms;
+    float ms_table[12];
+} eeg_tuning;
+EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
+                                const uint32_t* weight, eeg_algo algo, uint32_t reps, eeg_tuning* out);
+
 /* Allocation-free traversal run. No counterpart in the reference: it exists for callers that cannot
  * allocate device memory when they run a query -- plugins whose host application owns all GPU memory,
  * frameworks that route every allocation through their own pool, service loops where cudaMalloc's

@@ -84,6 +84,35 @@ def test_autotune_k(gpu):
     assert k2 == k
 
 
+@pytest.mark.parametrize("algo", ["bfs", "sssp", "sswp", "cc", "pr"])
+def test_autotune_k_and_variant(gpu, algo):
+    """eeg_autotune: a (K, variant) from the grid it times, every tried entry positive, CC never on
+    SYNC_PUSH_DD (another fixed point); the chosen configuration gives the oracle's answer."""
+    E = gpu
+    n = 1 << 12
+    s, d, w = E.gen_rmat(12, 8, seed=31, wmin=1, wmax=63)
+    if algo == "cc":
+        s, d, w = E.symmetrize(s, d, w)
+    t = E.autotune(n, s, d, w, algo=algo, reps=1)
+    assert t["K"] in (4, 8, 16) and t["ms"] > 0
+    assert (t["K"], t["variant"]) in t["table"] and all(v > 0 for v in t["table"].values())
+    tried_variants = {v for _, v in t["table"]}
+    if algo == "cc":
+        assert "sync_push_dd" not in tried_variants and len(t["table"]) == 9
+    else:
+        assert len(t["table"]) == 12
+    src = int(np.bincount(s, minlength=n).argmax())
+    if algo == "pr":
+        with E.VirtualGraph.build(n, s, d, None, K=t["K"], reverse_only=True) as vg:
+            x, _ = vg.run("pr", t["variant"])
+        xr, _ = oracle.pagerank(n, s, d)
+        assert np.abs(x / x.sum() - xr / xr.sum()).sum() <= 1e-6
+    else:
+        with E.VirtualGraph.build(n, s, d, w, K=t["K"]) as vg:
+            got, _ = vg.run(algo, t["variant"], src)
+        assert np.array_equal(got, oracle.expected(algo, t["variant"], n, s, d, w, src))
+
+
 @pytest.mark.parametrize("grid_queries", [1, 3, 100])
 def test_batch_whole_grid_queries(gpu, grid_queries):
     """The largest queries run one after another on the whole grid (bounded grid barrier), the rest on
