@@ -436,7 +436,8 @@ def bench_batch(args) -> None:
         torch.distributed.destroy_process_group()
     if rank != 0:
         return
-    line = {"metric": "batched queries/s (BFS/SSSP/SSWP mix over 256 graphs) vs the plain kernel looped per query",
+    line = {"metric": f"batched queries/s (BFS/SSSP/SSWP mix over {len(all_graphs)} graphs) vs the plain kernel "
+                      "looped per query",
             "value": round(nq / (bms * 1e-3), 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(bms, 3), "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded R-MAT mixture, generated in-process)",
