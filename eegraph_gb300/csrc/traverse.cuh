@@ -31,7 +31,14 @@
 namespace eeg {
 namespace trav {
 
-constexpr int T_TPB = 512;
+// CTA size per operator, two CTAs per SM: 512 threads (64 registers) for SSSP and SSWP; 384 threads
+// (85 registers) for BFS and CC, whose group of atomics then covers a whole 8-slot part. Measured on
+// R-MAT s22 with K = 8: BFS 0.383 / CC 1.24 ms at 384 against 0.395 / 1.30 ms at 512; SSSP 0.80 /
+// SSWP 0.74 ms at 384 against 0.75 / 0.73 ms at 512.
+template <int OP>
+__host__ __device__ constexpr int trav_tpb() {
+    return (OP == OP_BFS || OP == OP_CC) ? 384 : 512;
+}
 
 struct TravArgs {
     uint32_t n;
@@ -83,10 +90,10 @@ __device__ __forceinline__ bool unreached(uint32_t d) {
     if (OP == OP_SSWP) return d == 0u;
     return false;
 }
-// Slots whose atomics are issued together (value atomic + claim, 2 returned values each): the most that
-// fits the 64-register budget without slowing the kernel -- measured on R-MAT s22 with K = 8, groups of
-// 4 for BFS and SSSP (0.39 / 0.75 ms; 2: 0.40 / 0.77), 2 for SSWP and CC (0.73 / 1.30 ms; 4 spilled
-// registers: 0.80 / 1.50; 1: 0.76 / 1.34).
+// Slots whose atomics are issued together (value atomic + claim, 2 returned values each) under a
+// 64-register budget (512-thread CTAs; the batch kernel): the most that fits without slowing the kernel
+// -- measured on R-MAT s22 with K = 8, groups of 4 for BFS and SSSP (0.39 / 0.75 ms; 2: 0.40 / 0.77),
+// 2 for SSWP and CC (0.73 / 1.30 ms; 4 spilled registers: 0.80 / 1.50; 1: 0.76 / 1.34).
 template <int OP>
 __host__ __device__ constexpr int atomic_group() {
     return (OP == OP_SSWP || OP == OP_CC) ? 2 : 4;
@@ -179,7 +186,8 @@ __device__ __forceinline__ void warp_flush(const TravArgs& a, const uint32_t* bu
 // launch) reads the value the previous round settled; three piles rotate so that a pile's length is
 // reset two far rounds before it is written again.
 template <int OP, int K, bool TD, bool BK = false>
-__global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
+__global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
+    constexpr int T_TPB = trav_tpb<OP>();
     __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
     __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
     __shared__ uint32_t s_ctl[5];   // this round's control words, read once per CTA
@@ -421,7 +429,8 @@ __global__ void __launch_bounds__(T_TPB, 2) k_traverse(TravArgs a) {
             // read is no older than the round's start, and values move one way only) -- so the winner
             // appends the target, whoever improved it, and a target improved in a round is appended
             // exactly once.
-            constexpr int ATG = BK ? 2 : atomic_group<OP>();  // the far-pile path takes registers too
+            // the far-pile path takes registers too; the 384-thread shape has room for a whole part
+            constexpr int ATG = BK ? 2 : (trav_tpb<OP>() == 384 ? 8 : atomic_group<OP>());
             constexpr int ATB = K < ATG ? K : ATG;
 #pragma unroll
             for (int i0 = 0; i0 < K; i0 += ATB) {
@@ -544,6 +553,7 @@ template <int OP, int K, bool TD>
 eeg_status launch_one(const TravArgs& args, int device, uint32_t blocks_per_sm_req, cudaStream_t st) {
     constexpr bool CAN_BK = !TD && (OP == OP_SSSP || OP == OP_SSWP);
     auto kern = (CAN_BK && args.delta && !args.seed_all) ? k_traverse<OP, K, TD, CAN_BK> : k_traverse<OP, K, TD, false>;
+    constexpr int T_TPB = trav_tpb<OP>();
     int per_sm = 0;
     EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T_TPB, 0));
     if (per_sm <= 0) {
