@@ -31,13 +31,13 @@
 namespace eeg {
 namespace trav {
 
-// CTA size per operator, two CTAs per SM: 512 threads (64 registers) for SSSP and SSWP; 384 threads
-// (85 registers) for BFS and CC, whose group of atomics then covers a whole 8-slot part. Measured on
-// R-MAT s22 with K = 8: BFS 0.383 / CC 1.24 ms at 384 against 0.395 / 1.30 ms at 512; SSSP 0.80 /
-// SSWP 0.74 ms at 384 against 0.75 / 0.73 ms at 512.
+// CTA size per operator, two CTAs per SM: 384 threads (85 registers) for BFS, whose group of atomics
+// then covers a whole 8-slot part; 512 threads (64 registers) for the others. Measured with K = 8:
+// BFS 0.385 against 0.395 ms on R-MAT s22 and 2.2 against 2.6 ms on the 4096^2 grid; CC 1.35 against
+// 1.33 ms, SSSP 0.80 against 0.75 ms and SSWP 0.74 against 0.73 ms at 384 and 512 respectively.
 template <int OP>
 __host__ __device__ constexpr int trav_tpb() {
-    return (OP == OP_BFS || OP == OP_CC) ? 384 : 512;
+    return OP == OP_BFS ? 384 : 512;
 }
 
 struct TravArgs {
