@@ -395,16 +395,30 @@ __global__ void k_place(const uint32_t* __restrict__ key, const uint32_t* __rest
 }
 
 // Out-degree histogram of the input edges (with sym, of both directions); endpoints outside [0, n)
-// are counted nowhere (the transposed build reports them).
-__global__ void k_outdeg(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, uint64_t m, uint32_t n,
-                         uint32_t shift, int sym, uint32_t* __restrict__ deg) {
+// are counted nowhere (the transposed build reports them). The lowest OUTDEG_HOT ids count in shared
+// memory first, each CTA adding its non-zero counters at the end: generators that do not permute ids
+// (R-MAT) put their hubs there, and per-edge global atomics on a hub's counter queue at one L2 slice.
+constexpr uint32_t OUTDEG_HOT = 8192;
+__global__ void __launch_bounds__(256) k_outdeg(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b,
+                                                uint64_t m, uint32_t n, uint32_t shift, int sym,
+                                                uint32_t* __restrict__ deg) {
+    __shared__ uint32_t s_cnt[OUTDEG_HOT];
+    for (uint32_t i = threadIdx.x; i < OUTDEG_HOT; i += blockDim.x) s_cnt[i] = 0u;
+    __syncthreads();
+    auto count = [&](uint32_t v) {
+        if (v < OUTDEG_HOT) atomicAdd(&s_cnt[v], 1u);
+        else atomicAdd(&deg[v], 1u);
+    };
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
         const uint32_t s = a[e] - shift, t = b[e] - shift;
         if (s < n && t < n) {
-            atomicAdd(&deg[s], 1u);
-            if (sym) atomicAdd(&deg[t], 1u);
+            count(s);
+            if (sym) count(t);
         }
     }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < OUTDEG_HOT && i < n; i += blockDim.x)
+        if (s_cnt[i]) atomicAdd(&deg[i], s_cnt[i]);
 }
 // Largest degree and its smallest vertex, packed (degree << 32 | ~vertex) into one 64-bit max.
 __global__ void k_deg_best(const uint32_t* __restrict__ deg, uint32_t n, unsigned long long* best) {
@@ -466,7 +480,10 @@ eeg_status build_out_degrees(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, con
     EEG_TRY(T.get((void**)&best, sizeof(unsigned long long)));
     EEG_CUDA(cudaMemsetAsync(d->deg, 0, sizeof(uint32_t) * (size_t)(n + 1), st));
     EEG_CUDA(cudaMemsetAsync(best, 0, sizeof(unsigned long long), st));
-    if (m_in) k_outdeg<<<grid_for(m_in, vg->device), B_TPB, 0, st>>>(d_src, d_dst, m_in, n, shift, sym ? 1 : 0, d->deg);
+    // two CTAs per SM: each flushes its shared counters once
+    if (m_in)
+        k_outdeg<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m_in + 255) / 256, (uint64_t)sm_count(vg->device) * 2)),
+                   256, 0, st>>>(d_src, d_dst, m_in, n, shift, sym ? 1 : 0, d->deg);
     k_deg_best<<<grid_for(n, vg->device), B_TPB, 0, st>>>(d->deg, n, best);
     EEG_CUDA(cudaGetLastError());
     unsigned long long hb = 0;
