@@ -110,6 +110,10 @@ bool ArgumentParser::parse_impl(std::string* error) {
             timeoutMs = (unsigned)atoi(v);
         } else if (!strcmp(k, "--blocks-per-sm")) {
             blocksPerSM = (unsigned)atoi(v);
+        } else if (!strcmp(k, "--delta")) {
+            delta = (unsigned)atoi(v);
+        } else if (!strcmp(k, "--cc-components")) {
+            ccComponents = is_true(v);
         } else {
             *error = std::string("\nThere was an error parsing command line argument <") + k + ">\n" +
                      GenerateHelpString();
@@ -147,6 +151,8 @@ std::string ArgumentParser::GenerateHelpString() {
     str += "\n    [--tolerance]: PageRank bound on ||x - x*||_1 / ||x||_1 (Default: 1e-7)";
     str += "\n    [--timeout]: bound on any device-side wait in ms (Default: 10000)";
     str += "\n    [--blocks-per-sm]: cap on resident CTAs per SM for the persistent kernels";
+    str += "\n    [--delta]: SSSP/SSWP sync-push-dd bucketed rounds of this key width (Default: 0 = plain)";
+    str += "\n    [--cc-components]: CC as connected components, relaxing with weight 0 (Default: false)";
     str += "\n\n";
     return str;
 }

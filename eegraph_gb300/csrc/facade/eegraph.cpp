@@ -130,7 +130,8 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     Timer totalTimer;
     totalTimer.Start();
     if (en) eeg_energy_mark(en);
-    uint32_t flags = (algo == EEG_PR ? EEG_VG_REVERSE : 0u) | (um ? EEG_VG_MANAGED : 0u);
+    // PageRank reads only the transposed graph and the out-degrees
+    uint32_t flags = (algo == EEG_PR ? EEG_VG_REVERSE_ONLY : 0u) | (um ? EEG_VG_MANAGED : 0u);
     eeg_vgraph* vg = nullptr;
     check(eeg_vgraph_build_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), args.partSize, flags,
                                   nullptr, &vg),
@@ -142,6 +143,8 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     o.pr_accuracy = args.hasAcc ? args.acc : 0.f;
     o.timeout_ms = args.timeoutMs;
     o.blocks_per_sm = args.blocksPerSM;
+    o.delta = args.delta;
+    o.cc_components = args.ccComponents ? 1u : 0u;
     Result result;
     std::vector<uint> dist;
     std::vector<float> rank;

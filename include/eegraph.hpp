@@ -198,7 +198,8 @@ class UMVirtualGraph {
 // Command line: the reference's flags (--input --output --efile --estats --source --device --iteration
 // --debug --activity --variant --energy --um --accuracy) with the same defaults and the same
 // behaviour on errors (help text, exit(0)), plus --k {4,8,16}, --tolerance (PageRank L1 bound),
-// --timeout (ms, device waits) and --blocks-per-sm.
+// --timeout (ms, device waits), --blocks-per-sm, --delta (bucketed SSSP/SSWP rounds) and
+// --cc-components (CC as connected components).
 class ArgumentParser {
    public:
     int argc;
@@ -231,6 +232,8 @@ class ArgumentParser {
     float tolerance = 1e-7f;
     unsigned int timeoutMs = 10000;
     unsigned int blocksPerSM = 0;
+    unsigned int delta = 0;        // eeg_options.delta
+    bool ccComponents = false;     // eeg_options.cc_components
 
     ArgumentParser(int argc, char** argv, bool canHaveSource, bool canHaveItrs);
     bool Parse();

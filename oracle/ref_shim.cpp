@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <mutex>
 #include <new>
 #include <sstream>
 
@@ -36,6 +37,11 @@ void operator delete[](void* p) noexcept { free(p); }
 void operator delete[](void* p, size_t) noexcept { free(p); }
 
 namespace {
+
+// The reference's constructors print to std::cout, which is silenced by swapping its stream buffer --
+// process-wide state, so callers on several threads (the bench's reference arm) take turns here; the
+// timed seq_cpu calls run outside this lock.
+std::mutex g_cout_mu;
 
 struct Built {
     Graph g;
@@ -73,6 +79,7 @@ Built* make(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, co
         b->g.weights[e] = 1u;
     }
     b->g.num_edges = (uint)(m + pad);
+    std::lock_guard<std::mutex> lk(g_cout_mu);
     std::streambuf* old = std::cout.rdbuf();
     std::ostringstream sink;
     std::cout.rdbuf(sink.rdbuf());
@@ -89,6 +96,7 @@ extern "C" {
 // Graph::ReadGraph on a file: returns a handle; ref_graph_copy fills caller arrays.
 void* ref_graph_read(const char* path, int weighted) {
     Graph* g = new Graph(std::string(path), weighted != 0);
+    std::lock_guard<std::mutex> lk(g_cout_mu);
     std::streambuf* old = std::cout.rdbuf();
     std::ostringstream sink;
     std::cout.rdbuf(sink.rdbuf());

@@ -54,6 +54,18 @@ def test_unreadable_graph_reports():
     assert "Error reading graph" in r.stdout or "Graph file not read correctly" in r.stdout
 
 
+def test_extension_flags_parse():
+    """--delta and --cc-components are accepted (the run then stops at the missing graph file)."""
+    r = subprocess.run([str(BIN / "cc-main"), "--input", "/nonexistent/graph.el", "--cc-components", "true"],
+                       capture_output=True, text=True, timeout=60)
+    assert "<--cc-components>" not in r.stdout
+    assert "Error reading graph" in r.stdout or "Graph file not read correctly" in r.stdout
+    r = _run("--input", "/nonexistent/graph.el", "--delta", "16")
+    assert "<--delta>" not in r.stdout
+    assert "Error reading graph" in r.stdout or "Graph file not read correctly" in r.stdout
+    assert "--delta" in _run("--help").stdout and "--cc-components" in _run("--help").stdout
+
+
 def test_sweep_command_line():
     """sweep-main (the reference's src/main.cu measurement sweep): usage, bad options, bad variant."""
     exe = str(BIN / "sweep-main")
