@@ -166,3 +166,27 @@ def test_um_vertex_subgraph_equals_vertex_subgraph(tmp_path):
     r = subprocess.run([str(exe), str(g)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "SAME" in r.stdout and "PARTS " in r.stdout
+
+
+def test_cli_extension_flags(graph, tmp_path, gpu):
+    """--delta gives sssp-main the same distances; --cc-components gives cc-main the component minima of
+    the (undirected) input, by scipy."""
+    p, n, s, d, w = graph
+    src = int(np.bincount(s, minlength=n).argmax())
+    plain, bucketed = tmp_path / "plain.txt", tmp_path / "bucketed.txt"
+    _run("sssp-main", "--input", p, "--source", src, "--variant", "sync_push_dd", "--output", plain)
+    _run("sssp-main", "--input", p, "--source", src, "--variant", "sync_push_dd", "--output", bucketed,
+         "--delta", 16)
+    assert np.array_equal(_read_out(plain, np.uint64), _read_out(bucketed, np.uint64))
+    ss, ds, ws = gpu.symmetrize(s, d, w)
+    psym = tmp_path / "sym.wel"
+    _write_wel(psym, ss, ds, ws)
+    out = tmp_path / "cc.txt"
+    _run("cc-main", "--input", psym, "--output", out, "--cc-components", "true")
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    g = sp.coo_matrix((np.ones(ss.size), (ss.astype(np.int64), ds.astype(np.int64))), shape=(n, n))
+    _, comp = csgraph.connected_components(g, directed=False)
+    first = np.full(comp.max() + 1, n, np.int64)
+    np.minimum.at(first, comp, np.arange(n))
+    assert np.array_equal(_read_out(out, np.uint64), first[comp].astype(np.uint64))
