@@ -83,3 +83,45 @@ def test_bcsr_roundtrip(E, tmp_path):
         order = np.argsort(s, kind="stable")
         assert np.array_equal(v["src"], s[order]) and np.array_equal(v["dst"], d[order])
         assert np.array_equal(v["weight"], w[order] if weighted else np.ones_like(w))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_loader_fuzz_matches_oracle_parser(E, tmp_path, seed):
+    """Seeded random files mixing the golden files' quirks (comment and blank lines, tabs and runs of
+    spaces, CRLF, missing or float weights, extra columns, no final newline, 0- or 1-based ids), parsed
+    by the multi-threaded product loader and by the oracle's sequential restatement of ReadGraph (pinned
+    to the reference's own ReadGraph on the golden files): the same edge lists."""
+    rng = np.random.default_rng(seed)
+    n_lines = int(rng.integers(1, 3000))
+    base = int(rng.integers(0, 2))  # 1-based files have no id 0
+    eol = "\r\n" if rng.random() < 0.3 else "\n"
+    lines = []
+    for _ in range(n_lines):
+        r = rng.random()
+        if r < 0.05:
+            lines.append(rng.choice(["# comment", "% konect header", "", "   ", "c another"]))
+            continue
+        a, b = (int(x) for x in rng.integers(base, 5000, 2))
+        sep = rng.choice([" ", "\t", "  ", " \t "])
+        cols = [str(a), str(b)]
+        k = rng.random()
+        if k < 0.6:
+            cols.append(str(int(rng.integers(1, 100))))
+        elif k < 0.7:
+            cols.append(f"{rng.uniform(1, 50):.3f}")
+        elif k < 0.8:
+            cols += [str(int(rng.integers(1, 100))), "extra", "9"]
+        line = sep.join(cols)
+        if rng.random() < 0.1:
+            line += " "
+        lines.append(line)
+    text = eol.join(lines) + ("" if rng.random() < 0.2 else eol)
+    p = tmp_path / f"fuzz{seed}.wel"
+    p.write_bytes(text.encode())
+    want = oracle.parse(p)
+    for threads in (1, 4):
+        v = E.Graph.load(p, weighted=True, threads=threads).view()
+        assert (v["num_nodes"], v["num_edges"], int(v["has_zero_id"])) == \
+               (want["num_nodes"], want["src"].size, int(want["has_zero_id"])), (seed, threads)
+        assert np.array_equal(v["src"], want["src"]) and np.array_equal(v["dst"], want["dst"])
+        assert np.array_equal(v["weight"], want["weight"]), (seed, threads)
