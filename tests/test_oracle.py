@@ -146,3 +146,22 @@ def test_ppr_oracle_adjoint_against_finite_differences():
     assert np.abs(tot).max() <= 1e-12
     # normalised-weight gradient: d <x_u, lambda_v>
     assert np.allclose(r["gWn"], 0.85 * (r["X"][src] * r["L"][dst]).sum(1), rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_cc_labels_with_zero_weights_are_component_minima(seed):
+    """The CC oracle relaxed with weight 0 (what eeg_options.cc_components computes) labels each vertex
+    with the smallest id of its connected component: checked against scipy's components."""
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    rng = np.random.default_rng(seed)
+    n, m = 3000, int(rng.integers(500, 4000))
+    s = rng.integers(0, n, m).astype(np.uint32)
+    d = rng.integers(0, n, m).astype(np.uint32)
+    ss, ds = np.concatenate([s, d]), np.concatenate([d, s])
+    got = oracle.cc_labels(n, ss, ds, np.zeros(ss.size, np.uint32))
+    g = sp.coo_matrix((np.ones(ss.size), (ss.astype(np.int64), ds.astype(np.int64))), shape=(n, n))
+    _, comp = csgraph.connected_components(g, directed=False)
+    first = np.full(comp.max() + 1, n, np.int64)
+    np.minimum.at(first, comp, np.arange(n))
+    assert np.array_equal(got, first[comp].astype(np.uint32))
