@@ -95,18 +95,25 @@ class EnergyMeter:
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 50 ms (each line time-stamped) while the
+    sampler is open. summary() keeps the samples inside the window marked by start()/stop() -- the timed
+    region -- or every sample when no window was marked or no time stamp could be read."""
+
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device: int):
         self.device = device
         self.proc = None
         self.lines: list[str] = []
+        self.t0 = self.t1 = None
 
     def __enter__(self):
-        cmd = ["nvidia-smi", "-i", str(self.device),
-               "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"]
+        if self.proc is not None:  # already sampling (opened early, then used in a with block)
+            return self
+        cmd = ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+               "-lms", "50"]
         try:
             self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -119,6 +126,12 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def start(self):
+        self.t0 = time.time()
+
+    def stop(self):
+        self.t1 = time.time()
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -128,12 +141,26 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        import datetime
+
+        rows = []
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+            except ValueError:
+                ts = None
+            rows.append((ts, f[1:]))
+        window = "whole run"
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for r in rows if r[0] is not None and self.t0 - 0.05 <= r[0] <= self.t1 + 0.05]
+            if inside:
+                rows, window = inside, "timed region"
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in self.lines:
-            f = [x.strip() for x in l.split(",")]
-            if len(f) < 7:
-                continue
+        for _, f in rows:
             try:
                 sm.append(float(f[0]))
                 mx.append(float(f[1]))
@@ -145,7 +172,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "window": window}
 
 
 def reduce_job(total_ms: float, total_edges: float, world: int, device) -> tuple[float, float]:
@@ -215,6 +242,9 @@ def bench_gpu(args) -> None:
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     results: dict = {}
+    # the clock sampler runs from the warm-up on (nvidia-smi needs a moment to start) and keeps the
+    # samples stamped inside the timed region
+    clk = ClockSampler(local).__enter__()
     for _ in range(args.warmup):
         run_step(vg, vg_sym, vg_pr, source, outs, stream, results)
     torch.cuda.synchronize()
@@ -227,7 +257,8 @@ def bench_gpu(args) -> None:
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with clk:
+        clk.start()
         energy = EnergyMeter(local)
         for i in range(args.steps):
             flush.fill_(float(i))  # L2 flush between timed steps (outside the events)
@@ -242,6 +273,7 @@ def bench_gpu(args) -> None:
                 per_algo[a]["iters"].append(r["iterations"])
                 launches += r["launches"]
         torch.cuda.synchronize()
+        clk.stop()
         energy_line = energy.summary(args.steps, "timed steps (with their L2 flushes)")
         if world > 1:
             torch.distributed.barrier()
@@ -402,7 +434,9 @@ def bench_batch(args) -> None:
         for _ in range(args.warmup):
             b.run(out.data_ptr())
         energy = EnergyMeter(local)
+        clk.start()
         batch_ms = [b.run(out.data_ptr()) for _ in range(args.steps)]
+        clk.stop()
         energy_line = energy.summary(args.steps, "timed batch launches")
         batched = out.cpu().numpy().view(np.uint32).copy()
         offs = b.offsets()
@@ -528,6 +562,7 @@ def bench_ppr(args) -> None:
         for i in range(args.warmup + args.steps):
             if i == args.warmup:
                 energy = EnergyMeter(local)
+                clk.start()
             flush.zero_()
             torch.cuda.synchronize()
             ev0.record()
@@ -541,6 +576,7 @@ def bench_ppr(args) -> None:
                 step_ms.append(ev0.elapsed_time(ev1))
                 fwd.append(rf)
                 adj.append(ra)
+        clk.stop()
         energy_line = energy.summary(args.steps, "timed steps (with their L2 flushes)")
         # duality c^T x = (1-d) t^T lambda over this GPU's columns
         duality = abs(float((Gt.double() * X.double()).sum()) - float((Tt.double() * dT.double()).sum()))

@@ -47,3 +47,32 @@ def test_bench_help_names_every_workload():
         assert w in r.stdout
     for flag in ("--gpus", "--steps", "--warmup", "--impl", "--workload", "--ppr-columns"):
         assert flag in r.stdout
+
+
+def test_clock_sampler_keeps_the_timed_window():
+    """ClockSampler.summary(): samples stamped inside the start()/stop() window only; every sample when no
+    window was marked or a stamp cannot be read; throttle reasons reported by name."""
+    import datetime
+    import time
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    def line(t, sm, reasons=("Not Active",) * 4):
+        stamp = datetime.datetime.fromtimestamp(t).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+        return ", ".join([stamp, str(sm), "2070", "0x0", *reasons])
+
+    now = time.time()
+    c = bench.ClockSampler(0)
+    c.lines = [line(now - 5, 1000), line(now + 0.1, 2070), line(now + 0.2, 2070),
+               line(now + 0.3, 2070, ("Not Active", "Not Active", "Not Active", "Active")), line(now + 9, 500)]
+    whole = c.summary()
+    assert whole["samples"] == 5 and whole["window"] == "whole run"
+    c.t0, c.t1 = now, now + 0.35
+    timed = c.summary()
+    assert timed["samples"] == 3 and timed["window"] == "timed region"
+    assert timed["sm_mhz"] == 2070 and timed["sm_max_mhz"] == 2070 and timed["reasons"] == ["sw_power_cap"]
+    c.lines = ["garbled, 2070, 2070, 0x0, Not Active, Not Active, Not Active, Not Active"]
+    assert c.summary()["samples"] == 1 and c.summary()["window"] == "whole run"
+    c.lines = []
+    assert c.summary()["reasons"] == ["unavailable"]
