@@ -118,6 +118,9 @@ class ClockSampler:
             self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            import atexit
+
+            atexit.register(self.__exit__, None, None, None)  # no poller outlives the process
         except Exception:
             self.proc = None
         return self
@@ -133,7 +136,7 @@ class ClockSampler:
         self.t1 = time.time()
 
     def __exit__(self, *exc):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
