@@ -131,7 +131,7 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     totalTimer.Start();
     if (en) eeg_energy_mark(en);
     // PageRank reads only the transposed graph and the out-degrees
-    uint32_t flags = (algo == EEG_PR ? EEG_VG_REVERSE_ONLY : 0u) | (um ? EEG_VG_MANAGED : 0u);
+    uint32_t flags = (algo == EEG_PR ? (uint32_t)EEG_VG_REVERSE_ONLY : 0u) | (um ? (uint32_t)EEG_VG_MANAGED : 0u);
     eeg_vgraph* vg = nullptr;
     check(eeg_vgraph_build_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), args.partSize, flags,
                                   nullptr, &vg),
