@@ -14,9 +14,14 @@ Workload (one "step" = one pass of the hot path over the graph, every algorithm 
 Inputs are larger than L2 (the part arrays are ~0.7 GB) and L2 is also flushed (256 MB write)
 between timed steps.
 
---impl reference: the reference's CPU path (its seq_cpu sweeps -- oracle/_ref when built on this
-machine, else the oracle's C restatement of it; PageRank: the FP64 oracle, the reference has none) on
-a bounded sample (R-MAT scale 18, same parameters), all host threads, same metric and unit.
+cpu_baseline: the reference's CPU path on one core over the same graph (its seq_cpu sweeps, by the
+oracle's C restatement; PageRank: FP64 oracle sweeps, the reference has none); its outputs also check
+the GPU's outputs of the timed run (`parity`: integers bit-exact, PageRank normalised L1).
+
+--impl reference: the same CPU path on the same R-MAT scale-22 graph with all host threads, one step =
+the headline's five jobs at once (the four seq_cpu traversals on a core each, FP64 PageRank to the same
+stop on the remaining threads); the inputs come from the oracle's generator, so that arm loads no
+product library.
 """
 from __future__ import annotations
 
@@ -90,6 +95,9 @@ class EnergyMeter:
         r = self.session.end()
         if r is None:
             return {"unavailable": self.session.reason or "NVML energy counter not available"}
+        if r["joules"] <= 0.0:  # the counter did not advance over the region
+            return {"joules": None, "note": "below the energy counter's resolution over this region",
+                    "seconds": round(r["seconds"], 4), "covers": covers}
         return {"joules": round(r["joules"], 3), "joules_per_step": round(r["joules"] / max(steps, 1), 4),
                 "seconds": round(r["seconds"], 4), "avg_watts": round(r["avg_watts"], 1), "covers": covers}
 
@@ -281,6 +289,8 @@ def bench_gpu(args) -> None:
         if world > 1:
             torch.distributed.barrier()
     step_ms = [starts[i].elapsed_time(ends[i]) for i in range(args.steps)]
+    # the outputs of the last timed step, for the parity check against the reference CPU path
+    gpu_vals = {a: outs_t[a].cpu().numpy().view(np.float32 if a == "pr" else np.uint32).copy() for a, _ in ALGO_PLAN}
     total_ms = sum(step_ms)
     step_edges = sum(per_algo[a]["edges"][-1] for a, _ in ALGO_PLAN)
     total_edges = step_edges * args.steps
@@ -315,6 +325,9 @@ def bench_gpu(args) -> None:
         torch.cuda.synchronize()
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    # the end-to-end path's host outputs equal the device-resident run's (integers exactly, PageRank bitwise:
+    # same graph, same kernel)
+    e2e_equal = all(np.array_equal(host_out[a], gpu_vals[a]) for a, _ in ALGO_PLAN) if e2e_ms else None
     e2e_total_ms = sum(e2e_ms)
     if world > 1:
         tt = torch.tensor([e2e_total_ms], dtype=torch.float64, device=dev)
@@ -347,7 +360,6 @@ def bench_gpu(args) -> None:
         algo_summary[a]["dram_GB_per_launch"] = round(tr / 1e9, 3) if tr else None
     dom = max(algo_summary, key=lambda a: algo_summary[a]["kernel_ms"])
     kern_name = kern_names[dom]
-    wl = workload_name(scale, args.k, args.pr_k)
     ach = algo_summary[dom]["achieved_GBs"]
     line = {
         "metric": "GTEPS (sum over BFS,SSSP,SSWP,CC,PR of TEPS edges / device time)",
@@ -362,10 +374,7 @@ def bench_gpu(args) -> None:
         "vs_baseline": None,
         "dtype": "u32 (BFS/SSSP/SSWP/CC), f32 (PageRank)",
         "data": "synthetic (seeded R-MAT, generated in-process)",
-        "config": {"workload": wl, "scale": scale, "edge_factor": EF, "K": args.k, "pr_K": args.pr_k,
-                   "vertices": n, "edges": m,
-                   "cc_arcs": m_sym, "source": source, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (part arrays ~0.7 GB) and 256 MB L2 flush between timed steps"},
+        "config": headline_config(scale, args.k, args.pr_k, n, m, m_sym, source, world),
         "per_algo": algo_summary,
         "roofline": {"bound": "hbm", "kernel": kern_name, "achieved": ach, "peak": peak, "unit": "GB/s",
                      "frac": round(ach / peak, 4), "peak_source": peak_kind,
@@ -377,7 +386,10 @@ def bench_gpu(args) -> None:
         "energy": energy_line,
     }
     if not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(threads=1, budget_s=args.cpu_budget)
+        # the reference's CPU path on the same graph, one core; its outputs check the GPU's
+        line["cpu_baseline"], line["parity"] = cpu_baseline(n, (s, d, w), (ss, ds, ws), source, args.k, gpu_vals)
+        if e2e_ms:
+            line["parity"]["e2e_outputs_equal_device_outputs"] = e2e_equal
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -734,9 +746,9 @@ def bench_grid(args) -> None:
                     for _ in range(args.steps)]
             torch.cuda.synchronize()
             en = energy.summary(args.steps)
-            if "joules" in en:
+            if en.get("joules") is not None:
                 joules += en["joules"]
-            else:
+            elif "unavailable" in en:
                 energy_ok = False
             hl = vg.run(algo, variant, 0, out_device_ptr=out.data_ptr(), stream=stream, host_loop=True, delta=dl)[1]
             ms = statistics.median(r["kernel_ms"] for r in pers)
@@ -762,88 +774,133 @@ def bench_grid(args) -> None:
                        "vertices": n, "arcs": int(s.size)},
             "per_algo": per, "peak": peak, "peak_source": peak_kind, "clocks": clk.summary(),
             "energy": ({"joules": round(joules, 3), "joules_per_step": round(joules / args.steps, 4),
-                        "covers": "timed persistent runs of the three algorithms"} if energy_ok
-                       else {"unavailable": "NVML energy counter not available"})}
+                        "covers": "timed persistent runs of the three algorithms"} if energy_ok and joules > 0
+                       else {"joules": None, "note": "below the energy counter's resolution over these runs"}
+                       if energy_ok else {"unavailable": "NVML energy counter not available"})}
     print(json.dumps(line))
 
 
 # ---------------------------------------------------------------- CPU (reference) path
-def cpu_jobs(E, scale):
-    n, (s, d, w), (ss, ds, ws) = make_inputs(E, scale)
-    deg = np.bincount(s, minlength=n)
-    order = np.argsort(-deg, kind="stable")
-    return n, (s, d, w), (ss, ds, ws), order
+PR_SAMPLE_SWEEPS = 8  # PageRank sweeps the 1-core baseline times (the reference has no CPU PageRank)
 
 
-def cpu_run(job, n, g, gsym, use_ref):
-    """One CPU job; returns (TEPS edges, seconds of the algorithm alone)."""
+def make_inputs_cpu(scale: int):
+    """The headline's inputs made by the oracle's generator (identical arrays; no product library)."""
     import oracle
 
-    algo, source = job
-    s, d, w = g
-    if algo == "pr":
+    s, d, w = oracle.gen_rmat(scale, EF, seed=SEED, wmin=1, wmax=63)
+    ss, ds, ws = oracle.symmetrize(s, d, w)
+    return 1 << scale, (s, d, w), (ss, ds, ws)
+
+
+def headline_config(scale: int, K: int, pr_k: int, n: int, m: int, m_sym: int, source: int, world: int) -> dict:
+    """The `config` object of the headline line; both arms print the same one for the same workload."""
+    return {"workload": workload_name(scale, K, pr_k), "scale": scale, "edge_factor": EF, "K": K, "pr_K": pr_k,
+            "vertices": n, "edges": m, "cc_arcs": m_sym, "source": source, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (part arrays ~0.7 GB) and 256 MB L2 flush between timed steps"}
+
+
+class CpuPath:
+    """The reference's CPU path on one graph: its seq_cpu topology sweeps (the oracle's restatement of
+    src/{bfs,sssp,sswp,cc}.cu seq_cpu, on the lossless layout built once here, outside any timing) and,
+    for PageRank, which the reference has no CPU form of, the FP64 oracle's pull sweeps."""
+
+    def __init__(self, n, g, gsym, K: int = 8):
+        import oracle
+
+        self.o = oracle
+        self.n, self.K = n, K
+        s, d, w = g
+        self.m, self.m_sym = int(s.size), int(gsym[0].size)
+        self.layout = oracle.virtual_graph(n, s, d, w, K)
+        self.layout_sym = oracle.virtual_graph(n, *gsym, K)
+        self.csr_in = oracle.in_csr(n, s, d)  # in-edges by target, and the out-degrees
+
+    def traverse(self, algo: str, source: int):
+        """(values, TEPS edges, seconds of the sweeps)."""
+        lay = self.layout_sym if algo == "cc" else self.layout
+        vals, _, secs = self.o.seq_sweep_layout(algo, self.n, lay, source, self.K)
+        if algo == "cc":
+            return vals, float(self.m_sym), secs
+        reached = (vals != 0) if algo == "sswp" else (vals != self.o.INF)
+        return vals, float(self.csr_in[2][reached].sum()), secs
+
+    def pagerank(self, threads: int = 1, sweeps: int = 0, tol: float = PR_TOL * 0.15 / 0.85):
+        """(x, TEPS edges = sweeps * m, seconds); sweeps > 0 runs exactly that many sweeps."""
         t0 = time.perf_counter()
-        x, it = oracle.pagerank(n, s, d, 0.85, 1e-7 * 0.15 / 0.85)
-        return float(it) * s.size, time.perf_counter() - t0
-    if algo == "cc":
-        s, d, w = gsym
-    if use_ref:
-        out, secs = oracle.ref_seq_cpu(algo, n, s, d, w, source, timed=True)
-    else:
-        out, _, secs = oracle.seq_sweep(algo, n, s, d, w, source, timed=True)
-    if algo == "cc":
-        return float(s.size), secs
-    reached = (out != 0) if algo == "sswp" else (out != 4294967294)
-    return float(np.bincount(s, minlength=n)[reached].sum()), secs
+        x, it = self.o.pagerank_pull(self.csr_in, 0.85, 0.0 if sweeps else tol, sweeps or 100000, threads)
+        return x, float(it) * self.m, time.perf_counter() - t0
 
 
-def cpu_baseline(threads: int, budget_s: float, scale: int = SAMPLE_SCALE) -> dict:
-    """The reference's CPU path on a bounded sample: one pass of the five algorithms."""
-    import eegraph_gb300 as E
-    import oracle
+def parity_check(path: CpuPath, source: int, gpu_vals: dict, cpu_vals: dict, threads: int) -> dict:
+    """The GPU's outputs of the timed run against the reference CPU path's (bit-exact for the integer
+    algorithms) and PageRank against the FP64 oracle solved to 1e-11 (normalised L1)."""
+    out = {}
+    for a in ("bfs", "sssp", "sswp", "cc"):
+        if a in gpu_vals and a in cpu_vals:
+            bad = int((gpu_vals[a] != cpu_vals[a]).sum())
+            out[a] = "exact" if bad == 0 else f"{bad} vertices differ"
+    if "pr" in gpu_vals:
+        xr, _, _ = path.pagerank(threads=threads, tol=1e-11)
+        x = np.asarray(gpu_vals["pr"], np.float64)
+        out["pr_l1"] = float(np.abs(x / x.sum() - xr / xr.sum()).sum())
+        out["pr_ok"] = out["pr_l1"] <= 1e-6
+    out["against"] = (f"reference seq_cpu sweeps (oracle restatement) from vertex {source}, CC all seeded; "
+                      "PageRank FP64 oracle to 1e-11")
+    return out
 
-    use_ref = oracle.ref_available()
-    n, g, gsym, order = cpu_jobs(E, scale)
-    jobs = [("bfs", int(order[0])), ("sssp", int(order[0])), ("sswp", int(order[0])), ("cc", 0), ("pr", 0)]
-    tot_e, tot_t = 0.0, 0.0
-    t_start = time.perf_counter()
-    for j in jobs:
-        e, t = cpu_run(j, n, g, gsym, use_ref)
+
+def cpu_baseline(n, g, gsym, source, K, gpu_vals=None) -> tuple[dict, dict | None]:
+    """The reference's CPU path on ONE core over the headline's own graph: BFS, SSSP, SSWP (from the
+    max-out-degree vertex) and CC (every vertex seeded, symmetrised) by the seq_cpu sweeps, plus
+    PR_SAMPLE_SWEEPS PageRank sweeps of the FP64 oracle. Its outputs double as the parity check of the
+    GPU's outputs (gpu_vals) when given. Returns (cpu_baseline, parity)."""
+    path = CpuPath(n, g, gsym, K)
+    tot_e, tot_t, vals = 0.0, 0.0, {}
+    for algo in ("bfs", "sssp", "sswp", "cc"):
+        v, e, t = path.traverse(algo, source)
+        vals[algo] = v
         tot_e += e
         tot_t += t
-        if time.perf_counter() - t_start > budget_s:
-            break
-    return {"value": round(tot_e / tot_t / 1e9, 5), "unit": "GTEPS", "cores": threads,
-            "kind": "reference" if use_ref else "port",
-            "sample": f"R-MAT s{scale} ef{EF} (same a/b/c/d, seed, weights): BFS/SSSP/SSWP/CC via the reference's "
-                      f"seq_cpu sweeps ({'oracle/_ref' if use_ref else 'oracle C restatement'}), PR via the FP64 oracle"}
+    _, e, t = path.pagerank(threads=1, sweeps=PR_SAMPLE_SWEEPS)
+    tot_e += e
+    tot_t += t
+    line = {"value": round(tot_e / tot_t / 1e9, 5), "unit": "GTEPS", "cores": 1, "kind": "port",
+            "seconds": round(tot_t, 2),
+            "sample": f"the headline graph (R-MAT s{int(np.log2(n))}) itself: BFS/SSSP/SSWP/CC by the reference's "
+                      f"seq_cpu sweeps (oracle restatement, K={K}), PageRank {PR_SAMPLE_SWEEPS} FP64 sweeps (the "
+                      "reference has no CPU PageRank)"}
+    par = parity_check(path, source, gpu_vals, vals, threads=os.cpu_count() or 1) if gpu_vals else None
+    return line, par
 
 
 def bench_reference(args) -> None:
+    """The reference's CPU path on the headline's own graph with all host threads: one step runs the
+    headline's five jobs at once -- the four seq_cpu traversals on a core each and FP64 PageRank to the
+    headline's stop on the remaining threads -- and counts TEPS edges as the GPU arm does."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     import concurrent.futures as cf
 
-    import eegraph_gb300 as E
-    import oracle
-
-    use_ref = oracle.ref_available()
     threads = args.cpu_threads or os.cpu_count() or 1
-    n, g, gsym, order = cpu_jobs(E, SAMPLE_SCALE)
-    # one step = T concurrent independent jobs (all host threads): traversals from different sources, CC, PR
-    base = [("cc", 0), ("pr", 0)]
-    trav = [(a, int(order[i % 64])) for i in range(max(threads - 2, 3)) for a in ("bfs", "sssp", "sswp")][: max(threads - 2, 3)]
-    jobs = base + trav
+    scale = args.scale
+    n, g, gsym = make_inputs_cpu(scale)
+    source = int(np.bincount(g[0], minlength=n).argmax())
+    path = CpuPath(n, g, gsym, args.k)
+    pr_threads = max(1, threads - 4)
+    algos = [a for a, _ in ALGO_PLAN]
 
     def step():
         t0 = time.perf_counter()
-        with cf.ThreadPoolExecutor(threads) as ex:
-            res = list(ex.map(lambda j: cpu_run(j, n, g, gsym, use_ref), jobs))
-        return sum(e for e, _ in res), time.perf_counter() - t0
+        with cf.ThreadPoolExecutor(len(algos)) as ex:
+            futs = [ex.submit(path.pagerank, pr_threads) if a == "pr" else ex.submit(path.traverse, a, source)
+                    for a in algos]
+            edges = sum(f.result()[1] for f in futs)
+        return edges, time.perf_counter() - t0
 
-    for _ in range(args.warmup):
-        step()
+    for _ in range(args.warmup):  # warm-up: one BFS job per step (page-in of the layouts)
+        path.traverse("bfs", source)
     tot_e, tot_t = 0.0, 0.0
     for _ in range(args.steps):
         e, t = step()
@@ -856,12 +913,14 @@ def bench_reference(args) -> None:
         "value": round(value, 5), "unit": "GTEPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(tot_t / args.steps * 1e3, 2), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32 (BFS/SSSP/SSWP/CC), f64 (PageRank oracle)",
-        "data": "synthetic (seeded R-MAT)",
-        "config": {"workload": workload_name(SCALE, 8), "sample_scale": SAMPLE_SCALE, "threads": threads},
-        "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": threads,
-                         "kind": "reference" if use_ref else "port",
-                         "sample": f"per step {len(jobs)} concurrent jobs on R-MAT s{SAMPLE_SCALE} ef{EF}: "
-                                   "BFS/SSSP/SSWP seq_cpu from the top-degree vertices, CC seq_cpu, FP64 PageRank"},
+        "data": "synthetic (seeded R-MAT, generated in-process by the oracle's generator)",
+        "config": headline_config(scale, args.k, args.pr_k, n, path.m, path.m_sym, source, world),
+        "cpu_baseline": {"value": round(value, 5), "unit": "GTEPS", "cores": threads, "kind": "port",
+                         "sample": f"each step the headline's five jobs at once on R-MAT s{scale}: BFS/SSSP/SSWP "
+                                   f"from vertex {source} and CC (all seeded, symmetrised) by the reference's seq_cpu "
+                                   f"sweeps (oracle restatement; one core each), PageRank by the FP64 oracle to the "
+                                   f"headline's stop on {pr_threads} threads (the reference has no CPU PageRank); "
+                                   "warm-up steps run one BFS job each"},
         "e2e": {"value": round(value, 5), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

@@ -24,12 +24,25 @@ INF = 4294967294
 ALGO = {"bfs": 0, "sssp": 1, "sswp": 2, "cc": 3}
 
 
+def reference_dir() -> Path | None:
+    """The reference source tree: $EEG_REFERENCE_DIR, else a checkout named `reference` beside this
+    repository; None where neither holds the sources (the reference is then not built)."""
+    for cand in (os.environ.get("EEG_REFERENCE_DIR"), HERE.parent.parent / "reference"):
+        if cand and Path(cand, "src", "sssp.cu").exists():
+            return Path(cand)
+    return None
+
+
 def build(ref_dir: str | None = None) -> None:
     """Compile the restatement and, when the reference sources are present, the reference library."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    ref = ref_dir or os.environ.get("EEG_REFERENCE_DIR", "/root/reference")
-    if Path(ref, "src", "sssp.cu").exists():
+    ref = Path(ref_dir) if ref_dir else reference_dir()
+    if ref is not None and Path(ref, "src", "sssp.cu").exists():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={ref}"], check=True)
+
+
+def default_threads() -> int:
+    return max(1, min(64, os.cpu_count() or 1))
 
 
 _o = None
@@ -71,6 +84,19 @@ def lib():
         _o.orc_ppr_solve.argtypes = [u32, u64, vp, vp, vp, u32, vp, C.c_double, C.c_int, C.c_double, C.c_double,
                                      u64, vp]
         _o.orc_ppr_grads.argtypes = [u32, u64, vp, vp, vp, u32, vp, vp, C.c_double, vp, vp, vp]
+        _o.orc_pagerank_mt.restype = C.c_int64
+        _o.orc_pagerank_mt.argtypes = [u32, u64, vp, vp, C.c_double, C.c_double, u64, C.c_int, vp]
+        _o.orc_ppr_solve_mt.restype = C.c_int64
+        _o.orc_ppr_solve_mt.argtypes = [u32, u64, vp, vp, vp, u32, vp, C.c_double, C.c_int, C.c_double,
+                                        C.c_double, u64, C.c_int, vp]
+        _o.orc_in_csr.argtypes = [u32, u64, vp, vp, vp, vp, vp]
+        _o.orc_pagerank_pull.restype = C.c_int64
+        _o.orc_pagerank_pull.argtypes = [u32, vp, vp, vp, C.c_double, C.c_double, u64, C.c_int, vp]
+        _o.orc_gen_rmat.restype = C.c_int
+        _o.orc_gen_rmat.argtypes = [u32, u32, C.c_double, C.c_double, C.c_double, u64, u32, u32, C.c_int, vp, vp, vp]
+        _o.orc_gen_grid.restype = C.c_int
+        _o.orc_gen_grid.argtypes = [u32, C.c_double, C.c_double, u64, u32, u32, C.c_int, C.POINTER(u64), vp, vp, vp]
+        _o.orc_symmetrize.argtypes = [u64, vp, vp, vp, vp, vp, vp]
     return _o
 
 
@@ -139,6 +165,18 @@ def seq_sweep(algo, n, src, dst, w, source=0, K=8, wrap=False, max_sweeps=0, tim
     return (d, sweeps, secs) if timed else (d, sweeps)
 
 
+def seq_sweep_layout(algo, n, layout, source=0, K=8, wrap=False, max_sweeps=0):
+    """seq_sweep on a layout virtual_graph() already built: (values, sweeps, seconds of the sweeps)."""
+    import time
+
+    npn, el, pnp = layout
+    d = init_values(algo, n, source)
+    t0 = time.perf_counter()
+    sweeps = lib().orc_seq_sweep(ALGO[algo], n, pnp.size // 2, _vp(npn), _vp(el), _vp(pnp), K, int(wrap),
+                                 max_sweeps, _vp(d))
+    return d, sweeps, time.perf_counter() - t0
+
+
 def frontier_sweep(algo, n, src, dst, w, source=0, K=8, seed_all=False):
     npn, el, pnp = virtual_graph(n, src, dst, w, K)
     d = init_values(algo, n, source)
@@ -175,10 +213,28 @@ def cc_labels(n, src, dst, w):
     return d
 
 
-def pagerank(n, src, dst, damping=0.85, tol=1e-15, max_iter=100000):
+def pagerank(n, src, dst, damping=0.85, tol=1e-15, max_iter=100000, threads=1):
+    """FP64 PageRank fixed point (power iteration; same result for any thread count)."""
     x = np.empty(n, np.float64)
     src, dst = _u32(src), _u32(dst)
-    it = lib().orc_pagerank(n, src.size, _vp(src), _vp(dst), damping, tol, max_iter, _vp(x))
+    it = lib().orc_pagerank_mt(n, src.size, _vp(src), _vp(dst), damping, tol, max_iter, threads, _vp(x))
+    return x, it
+
+
+def in_csr(n, src, dst):
+    """(off[n+1], in-edge sources grouped by target, out-degrees) for pagerank_pull."""
+    src, dst = _u32(src), _u32(dst)
+    off, isrc, deg = np.empty(n + 1, np.uint64), np.empty(src.size, np.uint32), np.empty(n, np.uint32)
+    lib().orc_in_csr(n, src.size, _vp(src), _vp(dst), _vp(off), _vp(isrc), _vp(deg))
+    return off, isrc, deg
+
+
+def pagerank_pull(csr_in, damping=0.85, tol=1e-15, max_iter=100000, threads=1):
+    """pagerank() on a prepared in_csr(): the sweeps alone."""
+    off, isrc, deg = csr_in
+    n = deg.size
+    x = np.empty(n, np.float64)
+    it = lib().orc_pagerank_pull(n, _vp(off), _vp(isrc), _vp(deg), damping, tol, max_iter, threads, _vp(x))
     return x, it
 
 
@@ -187,7 +243,7 @@ def _f64(a, shape=None):
     return a if shape is None else a.reshape(shape)
 
 
-def ppr_solve(n, src, dst, w, b, transpose=False, damping=0.85, tol=1e-14, max_iter=100000):
+def ppr_solve(n, src, dst, w, b, transpose=False, damping=0.85, tol=1e-14, max_iter=100000, threads=1):
     """FP64 personalised PageRank (transpose=False: X = (1-d)B + d W^T X) or its adjoint
     (transpose=True: L = B + d W L) on row-normalised weights; b is n x C. Returns (Y, sweeps)."""
     src, dst, w = _u32(src), _u32(dst), _f64(w)
@@ -197,8 +253,8 @@ def ppr_solve(n, src, dst, w, b, transpose=False, damping=0.85, tol=1e-14, max_i
     C_ = b.shape[1]
     y = np.empty((n, C_), np.float64)
     scale = 1.0 if transpose else 1.0 - damping
-    it = lib().orc_ppr_solve(n, src.size, _vp(src), _vp(dst), _vp(w), C_, _vp(b), scale, int(transpose), damping,
-                             tol, max_iter, _vp(y))
+    it = lib().orc_ppr_solve_mt(n, src.size, _vp(src), _vp(dst), _vp(w), C_, _vp(b), scale, int(transpose), damping,
+                                tol, max_iter, threads, _vp(y))
     if it < 0:
         raise RuntimeError("oracle PPR solve did not converge")
     return y, it
@@ -217,12 +273,45 @@ def ppr_grads(n, src, dst, w, X, L, damping=0.85):
     return gWn, gw, gT
 
 
-def ppr(n, src, dst, w, T, G, damping=0.85, tol=1e-14):
+def ppr(n, src, dst, w, T, G, damping=0.85, tol=1e-14, threads=1):
     """Forward, adjoint and gradients in FP64. T: teleport (n x C), G: dLoss/dX (n x C)."""
-    X, itf = ppr_solve(n, src, dst, w, T, False, damping, tol)
-    L, ita = ppr_solve(n, src, dst, w, G, True, damping, tol)
+    X, itf = ppr_solve(n, src, dst, w, T, False, damping, tol, threads=threads)
+    L, ita = ppr_solve(n, src, dst, w, G, True, damping, tol, threads=threads)
     gWn, gw, gT = ppr_grads(n, src, dst, w, X, L, damping)
     return {"X": X, "L": L, "gWn": gWn, "gw": gw, "gT": gT, "sweeps": (itf, ita)}
+
+
+# ---------------------------------------------------------------- synthetic inputs (no product library)
+def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, wmin=1, wmax=63, weights=True, threads=0):
+    """The benchmark's seeded R-MAT edge list (identical to the product library's generator)."""
+    m = edge_factor << scale
+    src, dst = np.empty(m, np.uint32), np.empty(m, np.uint32)
+    w = np.empty(m, np.uint32) if weights else None
+    if lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, wmin, wmax, threads or default_threads(), _vp(src),
+                          _vp(dst), _vp(w)) != 0:
+        raise ValueError("invalid R-MAT parameters")
+    return src, dst, w
+
+
+def gen_grid(side, p_delete=0.1, shortcut_frac=0.001, seed=7, wmin=1, wmax=1000, threads=0):
+    """The benchmark's road-like grid: both arcs of every kept undirected edge, weights shared."""
+    cnt = C.c_uint64(0)
+    t = threads or default_threads()
+    if lib().orc_gen_grid(side, p_delete, shortcut_frac, seed, wmin, wmax, t, C.byref(cnt), None, None, None) != 0:
+        raise ValueError("invalid grid parameters")
+    m = cnt.value
+    src, dst, w = np.empty(m, np.uint32), np.empty(m, np.uint32), np.empty(m, np.uint32)
+    lib().orc_gen_grid(side, p_delete, shortcut_frac, seed, wmin, wmax, t, C.byref(cnt), _vp(src), _vp(dst), _vp(w))
+    return src, dst, w
+
+
+def symmetrize(src, dst, w=None):
+    src, dst = _u32(src), _u32(dst)
+    m = src.size
+    so, do = np.empty(2 * m, np.uint32), np.empty(2 * m, np.uint32)
+    wo = np.empty(2 * m, np.uint32) if w is not None else None
+    lib().orc_symmetrize(m, _vp(src), _vp(dst), _vp(_u32(w)) if w is not None else None, _vp(so), _vp(do), _vp(wo))
+    return so, do, wo
 
 
 def expected(algo, variant, n, src, dst, w, source):

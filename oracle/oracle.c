@@ -1,6 +1,7 @@
 /*
  * oracle.c -- CPU oracle for the EEGraph push-kernel path (declarations and scope in oracle.h).
- * TEST INFRASTRUCTURE ONLY. Plain C, single-threaded, written for clarity, not speed.
+ * TEST INFRASTRUCTURE ONLY. Plain C written for clarity; the FP64 PageRank solvers and the input
+ * generators also run on several threads (OpenMP) so that full-size checks finish in seconds.
  */
 #include "oracle.h"
 
@@ -438,37 +439,113 @@ void orc_widest(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst
     free_csr(&c);
 }
 
+/* Edges grouped by one endpoint (`key` = dst for a pull over in-edges, src for a pull over out-edges),
+ * stable: within a group the edges keep their input order, so a pull that adds them in group order
+ * adds them in the same order as a sequential scatter over the edge list would (same FP64 results). */
+typedef struct {
+    uint64_t* off; /* n + 1 */
+    uint64_t* eid; /* m: input edge index */
+} groups;
+
+static groups group_by(uint32_t n, uint64_t m, const uint32_t* key) {
+    groups g;
+    g.off = (uint64_t*)calloc((size_t)n + 1, sizeof(uint64_t));
+    g.eid = (uint64_t*)malloc((m ? m : 1) * sizeof(uint64_t));
+    for (uint64_t e = 0; e < m; ++e) g.off[key[e] + 1]++;
+    for (uint32_t v = 0; v < n; ++v) g.off[v + 1] += g.off[v];
+    uint64_t* pos = (uint64_t*)malloc(((size_t)n + 1) * sizeof(uint64_t));
+    memcpy(pos, g.off, ((size_t)n + 1) * sizeof(uint64_t));
+    for (uint64_t e = 0; e < m; ++e) g.eid[pos[key[e]]++] = e;
+    free(pos);
+    return g;
+}
+
+static void free_groups(groups* g) {
+    free(g->off);
+    free(g->eid);
+}
+
+/* Sums over fixed blocks of ORC_BLOCK vertices, added block by block: the same result for any thread count. */
+#define ORC_BLOCK 4096u
+
 int64_t orc_pagerank(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, double damping, double tol,
                      uint64_t max_iter, double* x) {
-    uint32_t* deg = (uint32_t*)calloc(n ? n : 1, sizeof(uint32_t));
-    double* y = (double*)malloc((n ? n : 1) * sizeof(double));
+    return orc_pagerank_mt(n, m, src, dst, damping, tol, max_iter, 1, x);
+}
+
+void orc_in_csr(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, uint64_t* off, uint32_t* isrc,
+                uint32_t* outdeg) {
+    memset(off, 0, ((size_t)n + 1) * sizeof(uint64_t));
+    memset(outdeg, 0, (size_t)n * sizeof(uint32_t));
+    for (uint64_t e = 0; e < m; ++e) {
+        off[dst[e] + 1]++;
+        outdeg[src[e]]++;
+    }
+    for (uint32_t v = 0; v < n; ++v) off[v + 1] += off[v];
+    uint64_t* pos = (uint64_t*)malloc(((size_t)n + 1) * sizeof(uint64_t));
+    memcpy(pos, off, ((size_t)n + 1) * sizeof(uint64_t));
+    for (uint64_t e = 0; e < m; ++e) isrc[pos[dst[e]]++] = src[e]; /* stable: input order per target */
+    free(pos);
+}
+
+int64_t orc_pagerank_pull(uint32_t n, const uint64_t* off, const uint32_t* isrc, const uint32_t* outdeg,
+                          double damping, double tol, uint64_t max_iter, int threads, double* x) {
+    if (threads < 1) threads = 1;
     double* c = (double*)malloc((n ? n : 1) * sizeof(double));
-    for (uint64_t e = 0; e < m; ++e) deg[src[e]]++;
+    const uint32_t nb = (n + ORC_BLOCK - 1) / ORC_BLOCK;
+    double* bdiff = (double*)calloc(nb ? nb : 1, sizeof(double));
+    double* bnorm = (double*)calloc(nb ? nb : 1, sizeof(double));
     for (uint32_t v = 0; v < n; ++v) x[v] = 1.0 - damping;
     int64_t it = 0;
     while ((uint64_t)it < max_iter) {
         ++it;
-        for (uint32_t v = 0; v < n; ++v) {
-            y[v] = 0.0;
-            c[v] = deg[v] ? x[v] / (double)deg[v] : 0.0;
+        int64_t v0;
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (v0 = 0; v0 < (int64_t)n; ++v0) c[v0] = outdeg[v0] ? x[v0] / (double)outdeg[v0] : 0.0;
+        int64_t b;
+        /* x_new[v] depends on c only, so x is updated in place block by block */
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+        for (b = 0; b < (int64_t)nb; ++b) {
+            double diff = 0.0, norm = 0.0;
+            const uint32_t lo = (uint32_t)b * ORC_BLOCK;
+            const uint32_t hi = lo + ORC_BLOCK < n ? lo + ORC_BLOCK : n;
+            for (uint32_t v = lo; v < hi; ++v) {
+                double y = 0.0;
+                for (uint64_t i = off[v]; i < off[v + 1]; ++i) y += c[isrc[i]];
+                const double nx = (1.0 - damping) + damping * y;
+                diff += nx > x[v] ? nx - x[v] : x[v] - nx;
+                norm += nx;
+                x[v] = nx;
+            }
+            bdiff[b] = diff;
+            bnorm[b] = norm;
         }
-        for (uint64_t e = 0; e < m; ++e) y[dst[e]] += c[src[e]];
         double diff = 0.0, norm = 0.0;
-        for (uint32_t v = 0; v < n; ++v) {
-            const double nx = (1.0 - damping) + damping * y[v];
-            diff += nx > x[v] ? nx - x[v] : x[v] - nx;
-            norm += nx;
-            x[v] = nx;
+        for (uint32_t k = 0; k < nb; ++k) {
+            diff += bdiff[k];
+            norm += bnorm[k];
         }
         if (diff <= tol * norm) break;
     }
-    free(deg);
-    free(y);
     free(c);
+    free(bdiff);
+    free(bnorm);
     return it;
 }
 
-/* ------------------------------------------------------------------ personalised PageRank (FP64) */
+int64_t orc_pagerank_mt(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, double damping, double tol,
+                        uint64_t max_iter, int threads, double* x) {
+    uint64_t* off = (uint64_t*)malloc(((size_t)n + 1) * sizeof(uint64_t));
+    uint32_t* isrc = (uint32_t*)malloc((m ? m : 1) * sizeof(uint32_t));
+    uint32_t* deg = (uint32_t*)malloc((n ? n : 1) * sizeof(uint32_t));
+    orc_in_csr(n, m, src, dst, off, isrc, deg);
+    const int64_t it = orc_pagerank_pull(n, off, isrc, deg, damping, tol, max_iter, threads, x);
+    free(off);
+    free(isrc);
+    free(deg);
+    return it;
+}
+
 static double* orc_out_sums(uint32_t n, uint64_t m, const uint32_t* src, const double* w) {
     double* s = (double*)calloc(n ? n : 1, sizeof(double));
     for (uint64_t e = 0; e < m; ++e) s[src[e]] += w[e];
@@ -478,30 +555,67 @@ static double* orc_out_sums(uint32_t n, uint64_t m, const uint32_t* src, const d
 int64_t orc_ppr_solve(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
                       const double* b, double scale_b, int transpose, double damping, double tol, uint64_t max_iter,
                       double* y) {
+    return orc_ppr_solve_mt(n, m, src, dst, w, C, b, scale_b, transpose, damping, tol, max_iter, 1, y);
+}
+
+int64_t orc_ppr_solve_mt(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w,
+                         uint32_t C, const double* b, double scale_b, int transpose, double damping, double tol,
+                         uint64_t max_iter, int threads, double* y) {
+    if (threads < 1) threads = 1;
     const size_t N = (size_t)n * C;
     double* s = orc_out_sums(n, m, src, w);
     double* z = (double*)malloc((N ? N : 1) * sizeof(double));
+    const uint32_t nb = (n + ORC_BLOCK - 1) / ORC_BLOCK;
+    double* bdiff = (double*)calloc(nb ? nb : 1, sizeof(double));
+    double* bnorm = (double*)calloc(nb ? nb : 1, sizeof(double));
+    /* forward: v gathers the rows of its in-neighbours u; adjoint: u gathers the rows of its out-neighbours v */
+    const uint32_t* to_key = transpose ? src : dst;
+    const uint32_t* from_key = transpose ? dst : src;
+    groups g = group_by(n, m, to_key);
+    uint32_t* from = (uint32_t*)malloc((m ? m : 1) * sizeof(uint32_t));
+    double* a = (double*)malloc((m ? m : 1) * sizeof(double));
+    for (uint64_t i = 0; i < m; ++i) {
+        const uint64_t e = g.eid[i];
+        from[i] = from_key[e];
+        a[i] = s[src[e]] == 0.0 ? 0.0 : damping * (w[e] / s[src[e]]);
+    }
     for (size_t i = 0; i < N; ++i) y[i] = scale_b * b[i];
     int64_t it = 0;
     int converged = 0;
     while ((uint64_t)it < max_iter) {
         ++it;
-        for (size_t i = 0; i < N; ++i) z[i] = scale_b * b[i];
-        for (uint64_t e = 0; e < m; ++e) {
-            const uint32_t u = src[e], v = dst[e];
-            if (s[u] == 0.0) continue;
-            const double a = damping * (w[e] / s[u]);
-            /* forward pushes u's row into v; the adjoint pulls v's row into u */
-            const uint32_t from = transpose ? v : u, to = transpose ? u : v;
-            const double* yr = y + (size_t)from * C;
-            double* zr = z + (size_t)to * C;
-            for (uint32_t k = 0; k < C; ++k) zr[k] += a * yr[k];
+        int64_t bk;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 16)
+        for (bk = 0; bk < (int64_t)nb; ++bk) {
+            const uint32_t lo = (uint32_t)bk * ORC_BLOCK;
+            const uint32_t hi = lo + ORC_BLOCK < n ? lo + ORC_BLOCK : n;
+            for (uint32_t v = lo; v < hi; ++v) {
+                double* zr = z + (size_t)v * C;
+                for (uint32_t k = 0; k < C; ++k) zr[k] = scale_b * b[(size_t)v * C + k];
+                for (uint64_t i = g.off[v]; i < g.off[v + 1]; ++i) {
+                    if (a[i] == 0.0 && s[transpose ? v : from[i]] == 0.0) continue; /* source without out-weight */
+                    const double* yr = y + (size_t)from[i] * C;
+                    for (uint32_t k = 0; k < C; ++k) zr[k] += a[i] * yr[k];
+                }
+            }
+        }
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (bk = 0; bk < (int64_t)nb; ++bk) {
+            const size_t lo = (size_t)bk * ORC_BLOCK * C;
+            const size_t hi = lo + (size_t)ORC_BLOCK * C < N ? lo + (size_t)ORC_BLOCK * C : N;
+            double diff = 0.0, norm = 0.0;
+            for (size_t i = lo; i < hi; ++i) {
+                diff += fabs(z[i] - y[i]);
+                norm += fabs(z[i]);
+                y[i] = z[i];
+            }
+            bdiff[bk] = diff;
+            bnorm[bk] = norm;
         }
         double diff = 0.0, norm = 0.0;
-        for (size_t i = 0; i < N; ++i) {
-            diff += fabs(z[i] - y[i]);
-            norm += fabs(z[i]);
-            y[i] = z[i];
+        for (uint32_t k = 0; k < nb; ++k) {
+            diff += bdiff[k];
+            norm += bnorm[k];
         }
         if (damping / (1.0 - damping) * diff <= tol * norm) {
             converged = 1;
@@ -510,6 +624,11 @@ int64_t orc_ppr_solve(uint32_t n, uint64_t m, const uint32_t* src, const uint32_
     }
     free(z);
     free(s);
+    free(a);
+    free(from);
+    free(bdiff);
+    free(bnorm);
+    free_groups(&g);
     return converged ? it : -1;
 }
 
@@ -535,4 +654,132 @@ void orc_ppr_grads(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* 
     free(r);
     free(g);
     free(s);
+}
+
+/* ------------------------------------------------------------------ synthetic inputs
+ * The seeded R-MAT and grid generators of the benchmark inputs, restated so that CPU-only code (the
+ * reference arm of the benchmark, oracle-side tests) makes the same graphs without loading the product
+ * library; tests check both give identical arrays. Counter-based: edge e depends only on (seed, e). */
+
+static uint64_t orc_mix64(uint64_t z) { /* SplitMix64 finaliser (Steele, Lea, Flood 2014) */
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint64_t orc_hash2(uint64_t a, uint64_t b) { return orc_mix64(a ^ orc_mix64(b + 0x632BE59BD9B4E019ull)); }
+
+int orc_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed, uint32_t wmin,
+                 uint32_t wmax, int threads, uint32_t* src, uint32_t* dst, uint32_t* weight) {
+    if (!src || !dst || scale == 0 || scale > 31 || a < 0 || b < 0 || c < 0 || a + b + c > 1.0 ||
+        (weight && wmax < wmin))
+        return -1;
+    if (threads < 1) threads = 1;
+    const uint64_t m = (uint64_t)edge_factor << scale;
+    const double two32 = 4294967296.0;
+    const uint64_t tA = (uint64_t)floor(a * two32);
+    const uint64_t tAB = (uint64_t)floor((a + b) * two32);
+    const uint64_t tABC = (uint64_t)floor((a + b + c) * two32);
+    const uint64_t range = (uint64_t)wmax - wmin + 1u;
+    int64_t e;
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (e = 0; e < (int64_t)m; ++e) {
+        const uint64_t s0 = orc_hash2(seed, (uint64_t)e);
+        uint32_t u = 0, v = 0;
+        uint64_t r = 0;
+        for (uint32_t l = 0; l < scale; ++l) { /* one quadrant choice per level, two per 64-bit draw */
+            if ((l & 1u) == 0) r = orc_mix64(s0 + 0x9E3779B97F4A7C15ull * (l / 2 + 1));
+            const uint64_t x = (l & 1u) ? (r >> 32) : (r & 0xFFFFFFFFull);
+            const uint32_t bit = 1u << (scale - 1 - l);
+            if (x < tA) {
+            } else if (x < tAB) {
+                v |= bit;
+            } else if (x < tABC) {
+                u |= bit;
+            } else {
+                u |= bit;
+                v |= bit;
+            }
+        }
+        src[e] = u;
+        dst[e] = v;
+        if (weight) weight[e] = wmin + (uint32_t)(orc_mix64(s0 ^ 0xA5A5A5A55A5A5A5Aull) % range);
+    }
+    return 0;
+}
+
+/* grid edge i: horizontal (r,c)-(r,c+1) for i < S(S-1), vertical (r,c)-(r+1,c) up to E = 2S(S-1), then shortcuts */
+static void grid_endpoints(uint64_t S, uint64_t E, uint64_t N, uint64_t seed, uint64_t i, uint32_t* u, uint32_t* v) {
+    if (i < S * (S - 1)) {
+        const uint64_t r = i / (S - 1), c = i % (S - 1);
+        *u = (uint32_t)(r * S + c);
+        *v = (uint32_t)(r * S + c + 1);
+    } else if (i < E) {
+        const uint64_t j = i - S * (S - 1);
+        const uint64_t r = j / S, c = j % S;
+        *u = (uint32_t)(r * S + c);
+        *v = (uint32_t)((r + 1) * S + c);
+    } else {
+        const uint64_t j = i - E;
+        *u = (uint32_t)(orc_hash2(seed ^ 0x5CA1AB1Eull, 2 * j) % N);
+        *v = (uint32_t)(orc_hash2(seed ^ 0x5CA1AB1Eull, 2 * j + 1) % N);
+    }
+}
+
+int orc_gen_grid(uint32_t side, double p_delete, double shortcut_frac, uint64_t seed, uint32_t wmin, uint32_t wmax,
+                 int threads, uint64_t* num_arcs, uint32_t* src, uint32_t* dst, uint32_t* weight) {
+    if (!num_arcs || side < 2 || (uint64_t)side * side > 0xFFFFFFFFull || p_delete < 0 || p_delete > 1 ||
+        shortcut_frac < 0 || wmax < wmin)
+        return -1;
+    if (threads < 1) threads = 1;
+    const uint64_t S = side, N = S * S, E = 2 * S * (S - 1);
+    const uint64_t nshort = (uint64_t)llround(shortcut_frac * (double)E);
+    const uint64_t thr = p_delete >= 1.0 ? ~0ull : (uint64_t)(p_delete * 18446744073709551616.0);
+    const uint64_t range = (uint64_t)wmax - wmin + 1u;
+    const uint64_t total = E + nshort, B = 1u << 16, nb = (total + B - 1) / B;
+    uint64_t* cnt = (uint64_t*)calloc(nb + 1, sizeof(uint64_t));
+    int64_t bk;
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (bk = 0; bk < (int64_t)nb; ++bk) {
+        uint64_t k = 0;
+        const uint64_t hi = ((uint64_t)bk + 1) * B < total ? ((uint64_t)bk + 1) * B : total;
+        for (uint64_t i = (uint64_t)bk * B; i < hi; ++i)
+            k += (i >= E || p_delete <= 0 || orc_mix64(orc_hash2(seed, i)) >= thr) ? 1 : 0;
+        cnt[bk + 1] = k;
+    }
+    for (uint64_t k = 0; k < nb; ++k) cnt[k + 1] += cnt[k];
+    *num_arcs = 2 * cnt[nb];
+    if (src && dst) {
+#pragma omp parallel for num_threads(threads) schedule(static)
+        for (bk = 0; bk < (int64_t)nb; ++bk) {
+            uint64_t o = 2 * cnt[bk];
+            const uint64_t hi = ((uint64_t)bk + 1) * B < total ? ((uint64_t)bk + 1) * B : total;
+            for (uint64_t i = (uint64_t)bk * B; i < hi; ++i) {
+                if (!(i >= E || p_delete <= 0 || orc_mix64(orc_hash2(seed, i)) >= thr)) continue;
+                uint32_t u, v;
+                grid_endpoints(S, E, N, seed, i, &u, &v);
+                const uint32_t w = wmin + (uint32_t)(orc_hash2(seed ^ 0x77EE77EEull, i) % range);
+                src[o] = u;
+                dst[o] = v;
+                src[o + 1] = v;
+                dst[o + 1] = u;
+                if (weight) weight[o] = weight[o + 1] = w;
+                o += 2;
+            }
+        }
+    }
+    free(cnt);
+    return 0;
+}
+
+void orc_symmetrize(uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w, uint32_t* so,
+                    uint32_t* d_o, uint32_t* wo) {
+    for (uint64_t e = 0; e < m; ++e) { /* the input arcs, then every arc reversed with its weight */
+        so[e] = src[e];
+        d_o[e] = dst[e];
+        so[m + e] = dst[e];
+        d_o[m + e] = src[e];
+        if (wo) wo[e] = wo[m + e] = w[e];
+    }
 }

@@ -85,6 +85,30 @@ int64_t orc_ppr_solve(uint32_t n, uint64_t m, const uint32_t* src, const uint32_
 void orc_ppr_grads(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w, uint32_t C,
                    const double* X, const double* L, double damping, double* gWn, double* gw, double* gT);
 
+/* Threaded forms of the two FP64 solvers (OpenMP where the oracle was built with it; the same result
+ * for every thread count: fixed sum orders). The plain forms above are these with one thread. */
+int64_t orc_pagerank_mt(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, double damping, double tol,
+                        uint64_t max_iter, int threads, double* x);
+/* PageRank in two steps: the in-edge CSR (sources grouped by target in input order, off[n+1]) and
+ * out-degrees once, then the pull sweeps on it (orc_pagerank_mt is the two in a row). */
+void orc_in_csr(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, uint64_t* off, uint32_t* isrc,
+                uint32_t* outdeg);
+int64_t orc_pagerank_pull(uint32_t n, const uint64_t* off, const uint32_t* isrc, const uint32_t* outdeg,
+                          double damping, double tol, uint64_t max_iter, int threads, double* x);
+int64_t orc_ppr_solve_mt(uint32_t n, uint64_t m, const uint32_t* src, const uint32_t* dst, const double* w,
+                         uint32_t C, const double* b, double scale_b, int transpose, double damping, double tol,
+                         uint64_t max_iter, int threads, double* y);
+
+/* Seeded synthetic inputs (the benchmark's R-MAT and road-like grid), identical to the product
+ * library's generators so CPU-only callers need not load it. Grid: call with src == NULL for the arc
+ * count first. Return 0, or -1 on invalid parameters. */
+int orc_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed, uint32_t wmin,
+                 uint32_t wmax, int threads, uint32_t* src, uint32_t* dst, uint32_t* weight);
+int orc_gen_grid(uint32_t side, double p_delete, double shortcut_frac, uint64_t seed, uint32_t wmin, uint32_t wmax,
+                 int threads, uint64_t* num_arcs, uint32_t* src, uint32_t* dst, uint32_t* weight);
+void orc_symmetrize(uint64_t m, const uint32_t* src, const uint32_t* dst, const uint32_t* w, uint32_t* so,
+                    uint32_t* d_o, uint32_t* wo);
+
 #ifdef __cplusplus
 }
 #endif

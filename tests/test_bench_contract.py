@@ -1,7 +1,7 @@
 """bench.py's JSON line, checked on CPU through the reference arm (`--impl reference` runs the
-reference's CPU path on a bounded sample and needs no GPU): every key the contract names, with the
-reference arm's own additions (`impl`, a `cpu_baseline` describing the run, an `e2e` that moves no
-bytes)."""
+reference's CPU path and needs no GPU; here on R-MAT scale 16 to stay quick): every key the contract
+names, with the reference arm's own additions (`impl`, a `cpu_baseline` describing the run, an `e2e`
+that moves no bytes); the arm maps no product library."""
 import json
 import subprocess
 import sys
@@ -10,12 +10,24 @@ from pathlib import Path
 ROOT = Path(__file__).resolve().parents[1]
 
 
-def _reference_line(*extra):
-    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
-                        "--cpu-threads", "2", *extra], capture_output=True, text=True, timeout=300, cwd=ROOT)
+# runs bench.py's main in this interpreter, then reports whether the product library was mapped
+_RUNNER = """
+import runpy, sys
+sys.argv = ["bench.py"] + sys.argv[1:]
+runpy.run_path("bench.py", run_name="__main__")
+maps = open("/proc/self/maps").read()
+print("PRODUCT_MAPPED", "libeegraph" in maps or "eegraph_gb300" in sys.modules)
+"""
+
+
+def _reference_line(*extra, product_mapped=False):
+    r = subprocess.run([sys.executable, "-c", _RUNNER, "--impl", "reference", "--steps", "1", "--warmup", "0",
+                        "--cpu-threads", "2", "--scale", "16", *extra], capture_output=True, text=True, timeout=300,
+                       cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1, r.stdout
+    assert f"PRODUCT_MAPPED {product_mapped}" in r.stdout, r.stdout[-500:]
     return json.loads(lines[0])
 
 
@@ -31,6 +43,11 @@ def test_reference_arm_line_has_the_contract_keys():
     assert d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 0
     assert d["scaling"] in ("weak", "strong")
     assert "workload" in d["config"]
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    c = d["config"]  # the GPU arm's config object for the same workload
+    assert c == bench.headline_config(16, 8, 16, 1 << 16, 16 << 16, 32 << 16, c["source"], 1)
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"] and cb["cores"] == 2
     assert cb["kind"] in ("reference", "port") and cb["sample"]

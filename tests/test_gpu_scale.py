@@ -1,0 +1,189 @@
+"""GPU parity at the sizes the benchmark numbers are quoted on (needs a GB300).
+
+* R-MAT scale 22, edge factor 16 (67,108,864 edges), a/b/c/d .57/.19/.19/.05, seed 1, weights U[1,63],
+  source = highest-out-degree vertex: BFS/SSSP/SSWP in every variant at K = 8, CC on the symmetrised
+  arc set (134 M arcs) in every variant, PageRank (pull over the transposed graph, K = 16, as the
+  benchmark builds it) in every variant; at K = 4 and K = 16 SSSP source-seeded and all-seeded and CC
+  all-seeded. Integer results bit-exact against the oracle (BFS, Dijkstra, max-min Dijkstra,
+  multi-source Dijkstra for the min-plus labels, and the frontier restatement for CC's source-seeded
+  variant); PageRank within 1e-6 normalised L1 of the FP64 oracle.
+* The 4096 x 4096 road-like grid (10 % of edges deleted, 0.1 % shortcuts, weights U[1,1000], seed 7)
+  from vertex 0: BFS, SSSP, SSWP with plain rounds, SSSP and SSWP with bucketed rounds (widths 8000
+  and 16, the benchmark's), BFS one launch per round: bit-exact.
+* Personalised PageRank on R-MAT scale 20 with 64 teleport vectors (the benchmark's inputs): four
+  columns of X and of dLoss/dT against the FP64 oracle within 1e-6 normalised L1, and the edge
+  gradients of a loss that weighs those four columns only (the other 60 columns are solved in the same
+  64-column launch with dLoss/dX = 0) within 1e-5.
+
+The oracles run on all host threads, several at once (they release the interpreter lock).
+"""
+import concurrent.futures as cf
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = ["async_push_td", "async_push_dd", "sync_push_td", "sync_push_dd"]
+PR_L1 = 1e-6
+THREADS = oracle.default_threads()
+
+
+def pr_l1(x, xr):
+    x = np.asarray(x, np.float64)
+    return float(np.abs(x / x.sum() - xr / xr.sum()).sum())
+
+
+def _mismatch(got, want):
+    bad = np.flatnonzero(got != want)
+    return f"{bad.size} vertices differ" + (f", first {int(bad[0])}: {int(got[bad[0]])} vs {int(want[bad[0]])}"
+                                             if bad.size else "")
+
+
+@pytest.fixture(scope="module")
+def rmat22(gpu):
+    E = gpu
+    n = 1 << 22
+    s, d, w = E.gen_rmat(22, 16, seed=1, wmin=1, wmax=63)
+    ss, ds, ws = E.symmetrize(s, d, w)
+    src = int(np.bincount(s, minlength=n).argmax())
+    with cf.ThreadPoolExecutor(6) as ex:
+        jobs = {"bfs": ex.submit(oracle.bfs, n, s, d, src),
+                "sssp": ex.submit(oracle.dijkstra, n, s, d, w, src),
+                "sswp": ex.submit(oracle.widest, n, s, d, w, src),
+                "cc": ex.submit(oracle.cc_labels, n, ss, ds, ws),
+                "cc_src": ex.submit(lambda: oracle.frontier_sweep("cc", n, ss, ds, ws, src, seed_all=False)[0]),
+                "pr": ex.submit(lambda: oracle.pagerank(n, s, d, 0.85, 1e-11, threads=THREADS)[0])}
+        want = {k: f.result() for k, f in jobs.items()}
+    return {"n": n, "g": (s, d, w), "sym": (ss, ds, ws), "src": src, "want": want}
+
+
+def test_rmat22_traversals_every_variant(gpu, rmat22):
+    n, (s, d, w), src = rmat22["n"], rmat22["g"], rmat22["src"]
+    with gpu.VirtualGraph.build(n, s, d, w, K=8) as vg:
+        assert vg.info()["max_degree_vertex"] == src
+        for algo in ("bfs", "sssp", "sswp"):
+            for variant in VARIANTS:
+                got, res = vg.run(algo, variant, src)
+                want = rmat22["want"][algo]
+                assert np.array_equal(got, want), (algo, variant, _mismatch(got, want))
+                if variant == "sync_push_dd":
+                    assert res["reached_vertices"] == int((want != (0 if algo == "sswp" else oracle.INF)).sum())
+
+
+def test_rmat22_cc_every_variant(gpu, rmat22):
+    n, (ss, ds, ws), src = rmat22["n"], rmat22["sym"], rmat22["src"]
+    with gpu.VirtualGraph.build(n, ss, ds, ws, K=8) as vg:
+        for variant in VARIANTS:
+            got, _ = vg.run("cc", variant, src)
+            want = rmat22["want"]["cc_src" if variant == "sync_push_dd" else "cc"]
+            assert np.array_equal(got, want), (variant, _mismatch(got, want))
+
+
+def test_rmat22_cc_built_on_device(gpu, rmat22):
+    """The benchmark's end-to-end step symmetrises on the device (EEG_VG_SYMMETRIZE) from the directed list."""
+    n, (s, d, w) = rmat22["n"], rmat22["g"]
+    with gpu.VirtualGraph.build(n, s, d, w, K=8, symmetrize=True) as vg:
+        got, _ = vg.run("cc", "async_push_dd", 0)
+    assert np.array_equal(got, rmat22["want"]["cc"]), _mismatch(got, rmat22["want"]["cc"])
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_rmat22_pagerank(gpu, rmat22, variant):
+    n, (s, d, _) = rmat22["n"], rmat22["g"]
+    with gpu.VirtualGraph.build(n, s, d, None, K=16, reverse=True) as vg:
+        x, res = vg.run("pr", variant, pr_tolerance=1e-7)
+    l1 = pr_l1(x, rmat22["want"]["pr"])
+    assert l1 <= PR_L1, (variant, l1)
+    assert res["iterations"] > 10
+
+
+def test_rmat22_pagerank_reverse_only(gpu, rmat22):
+    """The end-to-end step's PageRank graph: transposed parts and out-degrees only."""
+    n, (s, d, _) = rmat22["n"], rmat22["g"]
+    with gpu.VirtualGraph.build(n, s, d, None, K=16, reverse_only=True) as vg:
+        x, _ = vg.run("pr", "sync_push_td", pr_tolerance=1e-7)
+    assert pr_l1(x, rmat22["want"]["pr"]) <= PR_L1
+
+
+@pytest.mark.parametrize("K", [4, 16])
+def test_rmat22_other_part_sizes(gpu, rmat22, K):
+    n, (s, d, w), (ss, ds, ws), src = rmat22["n"], rmat22["g"], rmat22["sym"], rmat22["src"]
+    with gpu.VirtualGraph.build(n, s, d, w, K=K) as vg:
+        for variant in ("sync_push_dd", "async_push_dd"):  # source-seeded; every vertex seeded
+            got, _ = vg.run("sssp", variant, src)
+            assert np.array_equal(got, rmat22["want"]["sssp"]), (K, variant, _mismatch(got, rmat22["want"]["sssp"]))
+        got, _ = vg.run("bfs", "sync_push_dd", src)
+        assert np.array_equal(got, rmat22["want"]["bfs"]), (K, "bfs")
+    with gpu.VirtualGraph.build(n, ss, ds, ws, K=K) as vg:
+        got, _ = vg.run("cc", "async_push_dd", src)
+        assert np.array_equal(got, rmat22["want"]["cc"]), (K, "cc", _mismatch(got, rmat22["want"]["cc"]))
+
+
+def test_grid_4096(gpu):
+    E = gpu
+    side = 4096
+    n = side * side
+    s, d, w = E.gen_grid(side, 0.1, 0.001, seed=7, wmin=1, wmax=1000)
+    with cf.ThreadPoolExecutor(3) as ex:
+        jobs = {"bfs": ex.submit(oracle.bfs, n, s, d, 0), "sssp": ex.submit(oracle.dijkstra, n, s, d, w, 0),
+                "sswp": ex.submit(oracle.widest, n, s, d, w, 0)}
+        want = {k: f.result() for k, f in jobs.items()}
+    with E.VirtualGraph.build(n, s, d, w, K=8) as vg:
+        for algo in ("bfs", "sssp", "sswp"):
+            got, res = vg.run(algo, "sync_push_dd", 0)
+            assert np.array_equal(got, want[algo]), (algo, _mismatch(got, want[algo]))
+            assert res["iterations"] > 100
+        for algo, delta in (("sssp", 8000), ("sswp", 16)):
+            got, _ = vg.run(algo, "sync_push_dd", 0, delta=delta)
+            assert np.array_equal(got, want[algo]), (algo, delta, _mismatch(got, want[algo]))
+        got, res = vg.run("bfs", "sync_push_dd", 0, host_loop=True)
+        assert np.array_equal(got, want["bfs"]), ("bfs host loop", _mismatch(got, want["bfs"]))
+        assert res["launches"] >= res["iterations"]
+
+
+def _ppr_inputs(E, scale=20, cols=64, seed=1, seeds_per_col=32):
+    """The benchmark's personalised-PageRank inputs: R-MAT (scale, ef 16, seed 1), FP32 weights U(0,1],
+    `cols` teleport vectors uniform over 32 random vertices each, dLoss/dX ~ N(0,1)."""
+    n = 1 << scale
+    s, d, _ = E.gen_rmat(scale, 16, seed=seed, wmin=1, wmax=63)
+    rng = np.random.default_rng(seed)
+    w = (1.0 - rng.random(s.size)).astype(np.float32)
+    T = np.zeros((n, cols), np.float32)
+    for k in range(cols):
+        T[rng.choice(n, seeds_per_col, replace=False), k] = 1.0 / seeds_per_col
+    G = rng.standard_normal((n, cols)).astype(np.float32)
+    return n, np.asarray(s, np.uint32), np.asarray(d, np.uint32), w, T, G
+
+
+def _nl1_cols(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float((np.abs(a - b).sum(0) / np.maximum(np.abs(b).sum(0), 1e-300)).max())
+
+
+def _rel_l1(a, b):
+    a, b = np.asarray(a, np.float64).ravel(), np.asarray(b, np.float64).ravel()
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+def test_ppr_rmat20_64_columns(gpu):
+    E = gpu
+    n, s, d, w, T, G = _ppr_inputs(E)
+    pick = [0, 21, 42, 63]
+    Gs = np.zeros_like(G)
+    Gs[:, pick] = G[:, pick]
+    ref = oracle.ppr(n, s, d, w.astype(np.float64), T[:, pick], G[:, pick], damping=0.85, tol=1e-11,
+                     threads=THREADS)
+    with E.VirtualGraph.build(n, s, d, None, K=8, reverse=True, edge_ids=True) as vg, E.PPR(vg, 64) as p:
+        p.set_weights(w)
+        X, rf = p.forward(T)
+        out, ra = p.adjoint(Gs)
+    assert rf["iterations"] > 10 and ra["iterations"] > 10
+    assert _nl1_cols(X[:, pick], ref["X"]) <= 1e-6, _nl1_cols(X[:, pick], ref["X"])
+    assert _nl1_cols(out["dt"][:, pick], ref["gT"]) <= 1e-6, _nl1_cols(out["dt"][:, pick], ref["gT"])
+    rest = [k for k in range(64) if k not in pick]
+    assert not np.any(out["dt"][:, rest])  # dLoss/dX = 0 there: the adjoint of those columns is exactly 0
+    assert _rel_l1(out["dwn"], ref["gWn"]) <= 1e-5, _rel_l1(out["dwn"], ref["gWn"])
+    assert _rel_l1(out["dw"], ref["gw"]) <= 1e-5, _rel_l1(out["dw"], ref["gw"])

@@ -165,3 +165,42 @@ def test_cc_labels_with_zero_weights_are_component_minima(seed):
     first = np.full(comp.max() + 1, n, np.int64)
     np.minimum.at(first, comp, np.arange(n))
     assert np.array_equal(got, first[comp].astype(np.uint32))
+
+
+@pytest.mark.parametrize("scale,ef,seed", [(8, 16, 1), (13, 8, 3), (16, 16, 1)])
+def test_oracle_rmat_generator_equals_the_library(E, scale, ef, seed):
+    """The oracle makes the benchmark's inputs without the product library (the reference arm of the
+    benchmark must not load it); both generators give identical arrays."""
+    a = E.gen_rmat(scale, ef, seed=seed, wmin=1, wmax=63)
+    b = oracle.gen_rmat(scale, ef, seed=seed, wmin=1, wmax=63, threads=3)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    sa, sb = E.symmetrize(*a), oracle.symmetrize(*b)
+    for x, y in zip(sa, sb):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("side", [2, 37, 512])
+def test_oracle_grid_generator_equals_the_library(E, side):
+    a = E.gen_grid(side, 0.1, 0.001, seed=7, wmin=1, wmax=1000)
+    b = oracle.gen_grid(side, 0.1, 0.001, seed=7, wmin=1, wmax=1000, threads=4)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
+def test_threaded_fp64_solvers_equal_single_threaded():
+    """The threaded PageRank and PPR solves sum in fixed orders: identical results for any thread count."""
+    n = 1 << 12
+    s, d, _ = oracle.gen_rmat(12, 16, seed=5)
+    x1, i1 = oracle.pagerank(n, s, d, threads=1)
+    x4, i4 = oracle.pagerank(n, s, d, threads=4)
+    assert i1 == i4 and np.array_equal(x1, x4)
+    xp, ip = oracle.pagerank_pull(oracle.in_csr(n, s, d), threads=3)
+    assert ip == i1 and np.array_equal(xp, x1)
+    rng = np.random.default_rng(0)
+    w = 1.0 - rng.random(s.size)
+    b = rng.random((n, 3))
+    for tr in (False, True):
+        y1, k1 = oracle.ppr_solve(n, s, d, w, b, transpose=tr, threads=1)
+        y5, k5 = oracle.ppr_solve(n, s, d, w, b, transpose=tr, threads=5)
+        assert k1 == k5 and np.array_equal(y1, y5)
