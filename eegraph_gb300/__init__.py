@@ -65,7 +65,7 @@ class Options(C.Structure):
                 ("pr_accuracy", C.c_float), ("block_size", C.c_uint32), ("blocks_per_sm", C.c_uint32),
                 ("record_activity", C.c_uint32), ("timeout_ms", C.c_uint32), ("host_loop", C.c_uint32),
                 ("pr_hot_limit", C.c_uint32), ("delta", C.c_uint32), ("cc_components", C.c_uint32),
-                ("reserved", C.c_uint32 * 4)]
+                ("timeout_us", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
 class Tuning(C.Structure):
@@ -342,7 +342,7 @@ class VirtualGraph:
             pr_tolerance: float = 0.0, pr_damping: float = 0.0, blocks_per_sm: int = 0, timeout_ms: int = 0,
             activity_cap: int = 0, out: np.ndarray | None = None, out_device_ptr: int | None = None,
             stream: int | None = None, check: bool = True, host_loop: bool = False, pr_hot_limit: int = 0,
-            delta: int = 0, cc_components: bool = False):
+            delta: int = 0, cc_components: bool = False, timeout_us: int = 0):
         """Run one algorithm; returns (values, result-dict[, activity]). host_loop=True runs one launch
         per round with a host round trip in between (the reference's loop shape), for comparison.
         cc_components=True (CC only) relaxes with weight 0: connected components, not the reference's
@@ -360,6 +360,7 @@ class VirtualGraph:
         o.pr_hot_limit = pr_hot_limit
         o.delta = delta
         o.cc_components = 1 if cc_components else 0
+        o.timeout_us = timeout_us
         n = self.info()["num_nodes"]
         if out_device_ptr is not None:
             outp, on_dev, vals = C.c_void_p(out_device_ptr), 1, None

@@ -575,8 +575,14 @@ EEG_API eeg_status eeg_batch_run(eeg_batch* b, uint32_t* out, void* stream, floa
         BarrierWords bw{};
         EEG_CUDA(cudaMemcpy(&bw, b->d_bw, sizeof(bw), cudaMemcpyDeviceToHost));
         if (bw.status == DEV_TIMEOUT) {
-            set_last_error("eeg_batch_run: a grid barrier wait of the whole-grid phase exceeded the timeout");
-            return EEG_ERR_TIMEOUT;
+            // Some CTAs of the launch were not resident (another stream's kernels held SMs), so the
+            // whole-grid phase gave up and its queries' results are incomplete. Run the batch again with
+            // every query on the clusters, whose barriers need no more than the cluster co-resident.
+            const uint32_t keep = b->nbig;
+            EEG_TRY(eeg_batch_set_grid_queries(b, 0));
+            const eeg_status s = eeg_batch_run(b, out, stream, ms);
+            const eeg_status s2 = eeg_batch_set_grid_queries(b, keep);
+            return s != EEG_OK ? s : s2;
         }
     }
     return EEG_OK;

@@ -106,17 +106,16 @@ __device__ __forceinline__ bool grid_barrier(BarrierWords* bw, uint32_t& epoch, 
         __threadfence();
         atomicAdd(&bw->arrive, 1u);
         uint32_t ok = 1;
-        uint64_t t0 = 0;
+        const uint64_t t0 = global_timer_ns();  // the wait is measured from this CTA's arrival
         uint32_t spins = 0;
         while (true) {
             uint32_t cur = ld_acquire(&bw->arrive);
             if ((int32_t)(cur - target) >= 0) break;
             if (ld_relaxed(&bw->abort)) { ok = 0; break; }
             __nanosleep(32);
-            if ((++spins & 63u) == 0) {
-                uint64_t now = global_timer_ns();
-                if (t0 == 0) t0 = now;
-                else if (now - t0 > timeout_ns) {
+            if ((++spins & 7u) == 0) {
+                const uint64_t now = global_timer_ns();
+                if (now - t0 > timeout_ns) {
                     atomicCAS(&bw->status, (uint32_t)DEV_OK, (uint32_t)DEV_TIMEOUT);
                     atomicExch(&bw->abort, 1u);
                     ok = 0;

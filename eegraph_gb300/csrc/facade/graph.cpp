@@ -115,23 +115,38 @@ VertexSubgraph::~VertexSubgraph() { delete[] selected; }
 
 namespace {
 
+// One C-library draw, or two combined where the ids reach past RAND_MAX (every id stays reachable).
+uint draw(uint range) {
+    if ((unsigned long long)range <= (unsigned long long)RAND_MAX + 1ull) return (uint)rand() % range;
+    const unsigned long long hi = (unsigned long long)rand(), lo = (unsigned long long)rand();
+    return (uint)((hi * ((unsigned long long)RAND_MAX + 1ull) + lo) % range);
+}
+
 // pct of the n vertices: the source, then rand() draws seeded by `seed`, the first half of them from
 // the lowest fifth of the ids. Returns the number kept; `selected` must hold n zeroed flags.
+// The reference's loop (src/graph.cpp:148-164) never ends once the first half needs more distinct ids
+// than the lowest fifth holds (pct above about 0.4); here the draws move to the whole range when the
+// lowest fifth is used up, so every pct in [0, 1] ends, and the draws are the reference's whenever its
+// loop ends.
 uint select_vertices(uint n, float pct, int sourceNode, time_t seed, bool* selected) {
-    const uint target = (uint)(std::min(1.0, std::max(0.0, (double)pct)) * n);
+    const float p = std::min(1.0f, std::max(0.0f, pct));
+    const uint target = (uint)(p * n);  // a float product, as the reference's `pct * num_nodes`
     uint count = 0;
+    const uint low = n / 5 ? n / 5 : n;
+    uint low_taken = 0;  // selected ids below `low`
     if (n > 0 && sourceNode >= 0 && (uint)sourceNode < n) {
         selected[sourceNode] = true;
         count = 1;
+        low_taken = (uint)sourceNode < low ? 1 : 0;
     }
     srand((unsigned)seed);
-    const uint low = n / 5 ? n / 5 : n;
     while (count < target) {
-        const uint r = (uint)rand();
-        const uint v = count < target / 2 ? r % low : r % n;
+        const bool from_low = count < target / 2 && low_taken < low;
+        const uint v = draw(from_low ? low : n);
         if (!selected[v]) {
             selected[v] = true;
             ++count;
+            if (v < low) ++low_taken;
         }
     }
     return target;

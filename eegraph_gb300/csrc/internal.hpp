@@ -105,6 +105,12 @@ struct eeg_vgraph {
 
 namespace eeg {
 
+// Bound on device-side waits from the options: timeout_us when set, else timeout_ms (default 10 s).
+inline uint64_t wait_limit_ns(const eeg_options& o) {
+    if (o.timeout_us) return (uint64_t)o.timeout_us * 1000ull;
+    return (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
+}
+
 // allocation helpers (device or managed per graph)
 eeg_status vg_alloc(eeg_vgraph* vg, void** p, size_t bytes);
 void vg_free(eeg_vgraph* vg, void* p);

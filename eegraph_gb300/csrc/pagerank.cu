@@ -501,7 +501,7 @@ eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& 
     a.damping = damping;
     a.base = 1.0f - damping;
     a.tol = o.pr_tolerance > 0.f ? (double)o.pr_tolerance : 1e-7;
-    a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
+    a.timeout_ns = wait_limit_ns(o);
     a.inplace = (variant == EEG_ASYNC_PUSH_TD || variant == EEG_ASYNC_PUSH_DD) ? 1u : 0u;
 
     EEG_CUDA(cudaEventRecord(ws.ev[0], st));

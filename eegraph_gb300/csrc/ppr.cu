@@ -1039,7 +1039,7 @@ eeg_status solve(eeg_ppr* p, bool adjoint, const float* bsrc, const eeg_options&
     a.ctrl = p->ctrl;
     a.max_iters = o.max_iterations ? o.max_iterations : 10000u;
     a.tol = o.pr_tolerance > 0.f ? (double)o.pr_tolerance : 1e-7;
-    a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
+    a.timeout_ns = wait_limit_ns(o);
     EEG_CUDA(cudaMemsetAsync(p->ctrl, 0, sizeof(PRCtrl), st));
     EEG_TRY(reset_counters(d, st));
     switch (vg->K) {

@@ -101,7 +101,7 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
         a.fpile = ws.far;
         a.fflag = ws.far + 3 * (size_t)vg->n;
     }
-    a.timeout_ns = (uint64_t)(o.timeout_ms ? o.timeout_ms : 10000u) * 1000000ull;
+    a.timeout_ns = wait_limit_ns(o);
     a.it_start = 0;
     a.rounds_limit = o.host_loop ? 1u : 0u;
 

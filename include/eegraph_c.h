@@ -224,7 +224,10 @@ typedef struct eeg_options {
                                  weight, so label(v) = the smallest id in v's component when every vertex
                                  is seeded (ASYNC_* and SYNC_PUSH_TD) -- an extension, not the reference's
                                  min-plus labels (0, the default) */
-    uint32_t reserved[4];
+    uint32_t timeout_us;      /* bound on any device-side wait in microseconds; when nonzero it replaces
+                                 timeout_ms (sub-millisecond limits). A wait that runs out makes every CTA
+                                 leave and the call return EEG_ERR_TIMEOUT; the handle stays usable. */
+    uint32_t reserved[3];
 } eeg_options;
 
 typedef struct eeg_result {
@@ -291,7 +294,11 @@ EEG_API eeg_status eeg_batch_rounds(const eeg_batch* b, uint32_t* rounds);
  * index of the cluster that ran it (~0 for a whole-grid query) -- 3 values per query. */
 EEG_API eeg_status eeg_batch_query_times(const eeg_batch* b, unsigned long long* times);
 /* The first `count` queries in size order (largest graphs first) run one after another on the whole
- * grid before the rest are spread over the clusters (0 = none; the default). */
+ * grid before the rest are spread over the clusters (0 = none; the default). That phase waits at a
+ * grid-wide barrier, so it needs every CTA of the launch resident at once: with kernels of other
+ * streams holding SMs, some CTAs may not start, the wait gives up after 1 s, and eeg_batch_run then
+ * runs the batch once more with every query on the clusters (correct results, slower; *ms covers
+ * that second launch). Give the batch the device to itself when using this phase. */
 EEG_API eeg_status eeg_batch_set_grid_queries(eeg_batch* b, uint32_t count);
 EEG_API eeg_status eeg_batch_get_config(const eeg_batch* b, uint32_t* cluster_size, uint32_t* grid_queries);
 /* Autotuner: time the batch with 1, 2, 4 and 8 CTAs per query, each with 0, 1, 2, 4 ... 64 whole-grid
@@ -334,7 +341,9 @@ EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const ui
  * 256-byte blocks, exceeds the array (EEG_ERR_INVALID). The first call on a device looks up the array's
  * address (cudaGetSymbolAddress) -- make that first call before any stream capture. All calls on a device
  * share the array: calls that overlap on the GPU (unordered streams or threads) race and must be
- * serialised by the caller. Results equal eeg_run's; *iterations (may be NULL) receives the rounds. */
+ * serialised by the caller. Results equal eeg_run's with default eeg_options (there are none to pass:
+ * CC reads the weights, the round cap is n + 2, every device wait is bounded by 10 s, no bucketed rounds);
+ * *iterations (may be NULL) receives the rounds. */
 #define EEG_NOALLOC_SCRATCH_BYTES (32u << 20)
 EEG_API eeg_status eeg_run_noalloc(eeg_algo algo, eeg_variant variant, uint32_t num_nodes, uint64_t num_parts,
                                    uint32_t K, const uint32_t* vstart, const uint32_t* vowner, const uint32_t* vcol,

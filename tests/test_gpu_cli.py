@@ -65,6 +65,29 @@ def test_cli_output_and_lines(graph, tmp_path, exe, algo, variant):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("weighted", [True, False])
+def test_cli_binary_csr_input(graph, tmp_path, weighted):
+    """Subway's binary CSR files: `converter` turns the text list into .bwcsr (weighted) or .bcsr, and the
+    executables read them (Subway/tools/converter.cpp, Subway/shared/subway_graph.cu) with the same
+    results as the text file."""
+    p, n, s, d, w = graph
+    txt = tmp_path / ("g.wel" if weighted else "g.el")
+    with open(txt, "w") as f:
+        for a, b, c in zip(s.tolist(), d.tolist(), w.tolist()):
+            f.write(f"{a} {b} {c}\n" if weighted else f"{a} {b}\n")
+    _run("converter", txt)
+    binf = tmp_path / ("g.bwcsr" if weighted else "g.bcsr")
+    assert binf.exists()
+    src = int(np.bincount(s, minlength=n).argmax())
+    for exe, algo in ([("sssp-main", "sssp"), ("sswp-main", "sswp")] if weighted else [("bfs-main", "bfs")]):
+        for variant in ("sync_push_dd", "async_push_td"):
+            out = tmp_path / f"{algo}-{variant}.txt"
+            _run(exe, "--input", binf, "--source", src, "--variant", variant, "--output", out)
+            got = _read_out(out, np.uint64)
+            want = oracle.expected(algo, variant, n, s, d, w, src).astype(np.uint64)
+            assert np.array_equal(got, want), (exe, variant)
+
+
 def test_cli_pagerank_um_activity_energy(graph, tmp_path):
     p, n, s, d, w = graph
     out, ef, es = tmp_path / "pr.txt", tmp_path / "energy.csv", tmp_path / "stats.csv"

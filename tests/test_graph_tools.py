@@ -78,19 +78,48 @@ def test_vertex_subgraph_selection_and_induced_edges(tmp_path):
     k = next(i for i, l in enumerate(lines) if l.startswith("EDGES "))
     got_edges = [tuple(map(int, l.split())) for l in lines[k + 1:k + 1 + int(lines[k].split()[1])]]
     # the selection restated with the same C library's generator
-    libc = ctypes.CDLL(None)
     n = int(max(s.max(), d.max())) + 1
-    want_n = int(pct * n)
-    sel = {source}
-    libc.srand(ctypes.c_uint(seed))
-    while len(sel) < want_n:
-        rnd = libc.rand()
-        v = rnd % (n // 5) if len(sel) < want_n // 2 else rnd % n
-        sel.add(v)
+    sel = _selection(n, pct, source, seed)
     assert got_sel == sel
     want_edges = [(a, b, c) for a, b, c in zip(s.tolist(), d.tolist(), w.tolist()) if a in sel and b in sel]
     assert got_edges == want_edges
     assert "Subgraph number of edges = %d" % len(want_edges) in r.stdout
+
+
+def _selection(n, pct, source, seed):
+    """The reference's draw order (src/graph.cpp:148-164): the source, then rand() % (n/5) for the first
+    half, rand() % n after; once the lowest fifth is used up its draws move to the whole range (where
+    the reference's loop would not end)."""
+    libc = ctypes.CDLL(None)
+    want_n = int(np.float32(pct) * np.float32(n))  # the reference's float product
+    low = n // 5
+    sel = {source}
+    libc.srand(ctypes.c_uint(seed))
+    while len(sel) < want_n:
+        rnd = libc.rand()
+        from_low = len(sel) < want_n // 2 and sum(1 for v in sel if v < low) < low
+        sel.add(rnd % low if from_low else rnd % n)
+    return sel
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs a C++ compiler")
+@pytest.mark.parametrize("pct", [0.5, 0.9, 1.0])
+def test_vertex_subgraph_large_fractions_end(tmp_path, pct):
+    """Percentages above 40 % need more distinct ids in the first half than the lowest fifth holds:
+    the selection still ends, keeps exactly pct of the vertices, and matches the restated draws."""
+    p, s, d, w = _graph(tmp_path, n=300, m=2000, seed=8)
+    src = tmp_path / "drv.cpp"
+    src.write_text(DRIVER)
+    exe = tmp_path / "drv"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-o", str(exe), str(src), "-I", str(ROOT / "include"),
+                    "-L", str(LIB), "-leegraph_facade", "-leegraph", f"-Wl,-rpath,{LIB}", "-pthread"],
+                   check=True, timeout=120)
+    r = subprocess.run([str(exe), str(p), str(pct), "250", "77"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    got = set(int(x) for x in next(l for l in r.stdout.splitlines() if l.startswith("SEL")).split()[1:])
+    n = int(max(s.max(), d.max())) + 1
+    assert len(got) == int(np.float32(pct) * np.float32(n))
+    assert got == _selection(n, pct, 250, 77)
 
 
 def _subway_csr(src, dst, w):
