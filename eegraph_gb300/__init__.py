@@ -342,11 +342,12 @@ class VirtualGraph:
             pr_tolerance: float = 0.0, pr_damping: float = 0.0, blocks_per_sm: int = 0, timeout_ms: int = 0,
             activity_cap: int = 0, out: np.ndarray | None = None, out_device_ptr: int | None = None,
             stream: int | None = None, check: bool = True, host_loop: bool = False, pr_hot_limit: int = 0,
-            delta: int = 0, cc_components: bool = False, timeout_us: int = 0):
+            delta: int = 0, cc_components: bool = False, timeout_us: int = 0, pr_accuracy: float = 0.0):
         """Run one algorithm; returns (values, result-dict[, activity]). host_loop=True runs one launch
         per round with a host round trip in between (the reference's loop shape), for comparison.
         cc_components=True (CC only) relaxes with weight 0: connected components, not the reference's
-        min-plus labels."""
+        min-plus labels. pr_accuracy: the data-driven PageRank variants' activation threshold (the
+        reference's --accuracy; 0 = derived from pr_tolerance)."""
         a = ALGOS[algo] if isinstance(algo, str) else int(algo)
         v = VARIANTS[variant] if isinstance(variant, str) else int(variant)
         o = Options()
@@ -361,6 +362,7 @@ class VirtualGraph:
         o.delta = delta
         o.cc_components = 1 if cc_components else 0
         o.timeout_us = timeout_us
+        o.pr_accuracy = pr_accuracy
         n = self.info()["num_nodes"]
         if out_device_ptr is not None:
             outp, on_dev, vals = C.c_void_p(out_device_ptr), 1, None

@@ -109,6 +109,12 @@ static void free_ws(eeg_vgraph* vg) {
     vg_free(vg, w.pr_rcol);
     vg_free(vg, w.pr_info);
     if (w.pctrl) cudaFree(w.pctrl);
+    vg_free(vg, w.dd_r);
+    vg_free(vg, w.dd_x);
+    vg_free(vg, w.dd_amt);
+    vg_free(vg, w.dd_vq);
+    vg_free(vg, w.dd_pq);
+    if (w.ddctrl) cudaFree(w.ddctrl);
     if (w.stats) cudaFree(w.stats);
     if (w.ev[0]) cudaEventDestroy(w.ev[0]);
     if (w.ev[1]) cudaEventDestroy(w.ev[1]);
@@ -439,7 +445,8 @@ EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const ui
     eeg_tuning t{};
     t.ms = -1.f;
     for (float& x : t.ms_table) x = -1.f;
-    const uint32_t flags = algo == EEG_PR ? (uint32_t)EEG_VG_REVERSE_ONLY : 0u;
+    // PageRank: the transposed graph for the pull variants, the forward parts for the data-driven ones
+    const uint32_t flags = algo == EEG_PR ? (uint32_t)EEG_VG_REVERSE : 0u;
     const uint32_t* w = (algo == EEG_BFS || algo == EEG_PR) ? nullptr : weight;
     for (int i = 0; i < 3; ++i) {
         eeg_vgraph* vg = nullptr;
@@ -505,7 +512,8 @@ EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, u
     EEG_CUDA(cudaSetDevice(vg->device));
     eeg_status s;
     if (algo == EEG_PR) {
-        s = run_pagerank(vg, variant, o, st, &r);
+        const bool dd = variant == EEG_SYNC_PUSH_DD || variant == EEG_ASYNC_PUSH_DD;
+        s = dd ? run_pagerank_dd(vg, variant, o, st, &r) : run_pagerank(vg, variant, o, st, &r);
         if (s == EEG_OK || s == EEG_ERR_ITER_CAP) {
             if (out) {
                 EEG_CUDA(cudaMemcpyAsync(out, vg->ws.x, sizeof(float) * vg->n,
@@ -514,8 +522,14 @@ EEG_API eeg_status eeg_run(eeg_vgraph* vg, eeg_algo algo, eeg_variant variant, u
             }
             r.reached_vertices = vg->n;
             r.reached_edges = vg->m;
-            r.algorithmic_bytes = (double)r.iterations * (12.0 * vg->n + 8.0 * (double)vg->m);
-            r.gteps = r.kernel_ms > 0 ? (double)r.iterations * (double)vg->m / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
+            if (dd) {  // work-minimal bytes of the pushes made: per push its 4-byte target and 8-byte
+                       // residual update; per activation the vertex's residual, value, amount and row bounds
+                r.algorithmic_bytes = 12.0 * (double)r.edges_scanned + 32.0 * (double)r.updates;
+                r.gteps = r.kernel_ms > 0 ? (double)r.edges_scanned / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
+            } else {
+                r.algorithmic_bytes = (double)r.iterations * (12.0 * vg->n + 8.0 * (double)vg->m);
+                r.gteps = r.kernel_ms > 0 ? (double)r.iterations * (double)vg->m / (r.kernel_ms * 1e-3) / 1e9 : 0.0;
+            }
         }
         if (activity && activity_cap && res) r.num_activity = 0;
     } else {

@@ -130,8 +130,11 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     Timer totalTimer;
     totalTimer.Start();
     if (en) eeg_energy_mark(en);
-    // PageRank reads only the transposed graph and the out-degrees
-    uint32_t flags = (algo == EEG_PR ? (uint32_t)EEG_VG_REVERSE_ONLY : 0u) | (um ? (uint32_t)EEG_VG_MANAGED : 0u);
+    // PageRank's topology-driven pull reads only the transposed graph and the out-degrees; its data-driven
+    // variants push along out-edges, so they get the forward parts as well
+    const bool pr_dd = algo == EEG_PR && (args.variant == SYNC_PUSH_DD || args.variant == ASYNC_PUSH_DD);
+    uint32_t flags = (algo == EEG_PR ? (uint32_t)(pr_dd ? EEG_VG_REVERSE : EEG_VG_REVERSE_ONLY) : 0u) |
+                     (um ? (uint32_t)EEG_VG_MANAGED : 0u);
     eeg_vgraph* vg = nullptr;
     check(eeg_vgraph_build_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), args.partSize, flags,
                                   nullptr, &vg),

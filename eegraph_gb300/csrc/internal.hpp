@@ -60,6 +60,20 @@ struct PRCtrl {
     unsigned long long zero_in;  // vertices without in-edges (value stays 1-d)
 };
 
+// Control block of the data-driven PageRank kernel (residual frontier).
+struct PRDDCtrl {
+    BarrierWords bw;
+    uint32_t vlen[3];    // vertex-frontier lengths per round (rotating)
+    uint32_t plen[3];    // part-queue lengths per round (rotating)
+    uint32_t iterations;
+    uint32_t pad;
+    unsigned long long pushes;    // edge pushes over the run
+    unsigned long long parts;     // parts expanded over the run
+    unsigned long long consumed;  // residuals taken (vertex activations) over the run
+    double resid;        // sum of the residuals left at the end (error bound: resid / (1-d))
+    double norm;         // sum of the values at the end
+};
+
 struct Workspace {
     // traversal
     uint32_t* dist = nullptr;     // n
@@ -78,6 +92,13 @@ struct Workspace {
     uint32_t* pr_rcol = nullptr;  // transposed graph's neighbour ids as ranks (P_rev * K)
     uint2* pr_info = nullptr;     // n: (rank, out-degree) of each vertex, one load per finalisation
     PRCtrl* pctrl = nullptr;
+    // data-driven PageRank (residual frontier)
+    double* dd_r = nullptr;       // n: residuals
+    double* dd_x = nullptr;       // n: values (FP64 accumulation; the output is written to x)
+    double* dd_amt = nullptr;     // n: push amount of each vertex activated in the current round
+    uint32_t* dd_vq = nullptr;    // 2n: vertex frontiers (double-buffered)
+    uint32_t* dd_pq = nullptr;    // P: part queue of the current round
+    PRDDCtrl* ddctrl = nullptr;
     // misc
     unsigned long long* stats = nullptr;  // reached counters
     cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -125,6 +146,8 @@ eeg_status build_out_degrees(eeg_vgraph* vg, VDir* d, const uint32_t* d_src, con
 eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t source, const eeg_options& o,
                          cudaStream_t st, eeg_result* res, uint32_t* activity_host, uint32_t activity_cap);
 eeg_status run_pagerank(eeg_vgraph* vg, eeg_variant variant, const eeg_options& o, cudaStream_t st, eeg_result* res);
+eeg_status run_pagerank_dd(eeg_vgraph* vg, eeg_variant variant, const eeg_options& o, cudaStream_t st,
+                           eeg_result* res);
 eeg_status reached_stats(eeg_vgraph* vg, int op, const uint32_t* d_dist, cudaStream_t st, uint64_t* n_r, uint64_t* m_r);
 
 }  // namespace eeg

@@ -103,7 +103,7 @@ def test_autotune_k_and_variant(gpu, algo):
         assert len(t["table"]) == 12
     src = int(np.bincount(s, minlength=n).argmax())
     if algo == "pr":
-        with E.VirtualGraph.build(n, s, d, None, K=t["K"], reverse_only=True) as vg:
+        with E.VirtualGraph.build(n, s, d, None, K=t["K"], reverse=True) as vg:
             x, _ = vg.run("pr", t["variant"])
         xr, _ = oracle.pagerank(n, s, d)
         assert np.abs(x / x.sum() - xr / xr.sum()).sum() <= 1e-6

@@ -101,6 +101,21 @@ def test_cli_pagerank_um_activity_energy(graph, tmp_path):
     assert ("Energy consumed" in stdout and es.exists()) or "Energy unavailable" in stdout
 
 
+@pytest.mark.parametrize("variant", ["sync_push_dd", "async_push_dd"])
+def test_cli_pagerank_data_driven_accuracy(graph, tmp_path, variant):
+    """pr-main's data-driven variants take the reference's --accuracy as their activation threshold: a
+    coarse threshold stops early with a larger error, a fine one meets the oracle."""
+    p, n, s, d, w = graph
+    xr, _ = oracle.pagerank(n, s, d)
+    errs = []
+    for acc in ("0.01", "1e-9"):
+        out = tmp_path / f"pr-{acc}.txt"
+        _run("pr-main", "--input", p, "--variant", variant, "--output", out, "--accuracy", acc)
+        x = _read_out(out, np.float64)
+        errs.append(np.abs(x / x.sum() - xr / xr.sum()).sum())
+    assert errs[1] <= 1e-5 < errs[0]
+
+
 def test_cli_one_based_file_and_activity(tmp_path, gpu):
     s, d, w = gpu.gen_rmat(10, 8, seed=9, wmin=1, wmax=63)
     p = tmp_path / "one.wel"

@@ -49,9 +49,10 @@ def test_golden_graphs_all_variants(gpu, name, c, K):
                     # identical to what the reference's own seq_cpu returned
                     assert np.array_equal(got, c[f"ref_{algo}"]), (algo, variant)
         if c["src"].size:
-            x, res = vg.run("pr", "sync_push_td")
             xr, _ = oracle.pagerank(n, c["src"], c["dst"])
-            assert pr_l1(x, xr) <= PR_L1
+            for variant in VARIANTS:
+                x, res = vg.run("pr", variant)
+                assert pr_l1(x, xr) <= PR_L1, (variant, pr_l1(x, xr))
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
@@ -105,15 +106,55 @@ def test_grid_high_diameter(gpu):
         assert res["iterations"] > side  # many rounds, one launch
 
 
-@pytest.mark.parametrize("variant", ["sync_push_td", "async_push_td"])
-def test_pagerank_variants(gpu, variant):
+@pytest.mark.parametrize("K", [4, 8, 16])
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_pagerank_variants(gpu, variant, K):
+    """Topology-driven variants: Jacobi pull sweeps; data-driven variants: the residual frontier
+    (pushes along out-edges, activation threshold derived from the tolerance)."""
     n = 1 << 14
     s, d, _ = gpu.gen_rmat(14, 16, seed=9)
-    with gpu.VirtualGraph.build(n, s, d, None, K=8, reverse=True) as vg:
+    with gpu.VirtualGraph.build(n, s, d, None, K=K, reverse=True) as vg:
         x, res = vg.run("pr", variant)
     xr, _ = oracle.pagerank(n, s, d)
-    assert pr_l1(x, xr) <= PR_L1
+    assert pr_l1(x, xr) <= PR_L1, (variant, pr_l1(x, xr))
     assert res["iterations"] > 5
+    if variant.endswith("_dd"):
+        # every residual left is below the threshold tol*(1-d)^2: the bound ||x*-x||_1 <= resid/(1-d)
+        assert res["pr_residual"] / 0.15 <= 1e-7 * res["pr_l1_norm"] * 1.0001
+        assert res["edges_scanned"] > s.size  # round 0 pushes along every edge, later rounds some
+
+
+@pytest.mark.parametrize("variant", ["sync_push_dd", "async_push_dd"])
+def test_pagerank_dd_accuracy_threshold(gpu, variant):
+    """An explicit activation threshold (the reference's --accuracy): fewer rounds and pushes the larger
+    it is, every residual left below it, and the error within the bound it implies,
+    ||x* - x||_1 <= (sum of residuals) / (1-d)."""
+    n = 1 << 14
+    s, d, _ = gpu.gen_rmat(14, 16, seed=9)
+    xr, _ = oracle.pagerank(n, s, d)
+    prev = None
+    with gpu.VirtualGraph.build(n, s, d, None, K=8, reverse=True) as vg:
+        for acc in (1e-2, 1e-4, 1e-6):
+            x, res = vg.run("pr", variant, pr_accuracy=acc)
+            err = float(np.abs(np.asarray(x, np.float64) - xr).sum())
+            assert err <= res["pr_residual"] / 0.15 * 1.001 + 1e-5 * np.abs(xr).sum(), (acc, err)
+            assert res["pr_residual"] <= n * acc
+            if prev is not None:
+                assert res["edges_scanned"] > prev["edges_scanned"] and res["iterations"] >= prev["iterations"]
+            prev = res
+        x0, res0 = vg.run("pr", variant, pr_accuracy=0.2)  # above the initial residual 1-d: nothing moves
+        assert res0["edges_scanned"] == 0 and not np.any(x0)
+
+
+def test_pagerank_dd_needs_the_forward_parts(gpu):
+    n = 1 << 10
+    s, d, _ = gpu.gen_rmat(10, 8, seed=2)
+    with gpu.VirtualGraph.build(n, s, d, None, K=8, reverse_only=True) as vg:
+        _, res = vg.run("pr", "sync_push_dd", check=False)
+        assert res["status"] == gpu.ERR_INVALID
+        x, res = vg.run("pr", "sync_push_td")  # the pull still runs on it
+    xr, _ = oracle.pagerank(n, s, d)
+    assert pr_l1(x, xr) <= PR_L1
 
 
 def test_builder_layout(gpu):
