@@ -14,6 +14,12 @@ Workload (one "step" = one pass of the hot path over the graph, every algorithm 
 Inputs are larger than L2 (the part arrays are ~0.7 GB) and L2 is also flushed (256 MB write)
 between timed steps.
 
+The default (one GPU) line also carries `grid`, `batch` and `ppr`: the lines of the other workloads
+(--workload grid|batch|ppr) measured after the headline with fewer timed steps -- the 4096^2 road-like
+grid against one launch per round, the 256-graph query batch against the plain kernel looped per query
+(its wall time and the sum of its kernel times), the 64-column personalised-PageRank adjoint against the
+single-column kernels looped per teleport vector. --no-extras leaves them out.
+
 cpu_baseline: the reference's CPU path on one core over the same graph (its seq_cpu sweeps, by the
 oracle's C restatement; PageRank: FP64 oracle sweeps, the reference has none); its outputs also check
 the GPU's outputs of the timed run (`parity`: integers bit-exact, PageRank normalised L1).
@@ -70,15 +76,32 @@ def load_peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
+# the sources each measured kernel is compiled from (a traffic figure is used only while they are unchanged)
+KERNEL_SOURCES = {"k_traverse": ["traverse.cuh", "traverse_host.cu", "common.cuh"],
+                  "k_pagerank": ["pagerank.cu", "common.cuh"], "k_ppr_rows": ["ppr.cu", "common.cuh"]}
+
+
+def kernel_source_sha(kernel: str) -> str:
+    import hashlib
+
+    h = hashlib.sha1()
+    for f in KERNEL_SOURCES[kernel.split("<")[0]]:
+        h.update((ROOT / "eegraph_gb300" / "csrc" / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
 def load_traffic(kernel: str, workload: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary (profiles/traffic.json), or None
+    when there is none or it was measured on other sources of the kernel than the ones built here."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
         return None
     try:
         t = json.loads(p.read_text())
         e = t.get(workload, {}).get(kernel)
-        return None if e is None else float(e["dram_bytes_per_launch"])
+        if e is None or e.get("source_sha") != kernel_source_sha(kernel):
+            return None
+        return float(e["dram_bytes_per_launch"])
     except Exception:
         return None
 
@@ -385,6 +408,11 @@ def bench_gpu(args) -> None:
         "clocks": clk.summary(),
         "energy": energy_line,
     }
+    if world == 1 and not args.no_extras:
+        vg.close()
+        vg_sym.close()
+        vg_pr.close()
+        line.update(extras(args))
     if not args.no_cpu_baseline:
         # the reference's CPU path on the same graph, one core; its outputs check the GPU's
         line["cpu_baseline"], line["parity"] = cpu_baseline(n, (s, d, w), (ss, ds, ws), source, args.k, gpu_vals)
@@ -393,6 +421,32 @@ def bench_gpu(args) -> None:
     print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def extras(args) -> dict:
+    """Summaries of the other configurations the measurement plan names, measured after the headline in
+    the same run (one GPU): the 4096^2 road-like grid (persistent kernel vs one launch per round), the
+    256-graph query batch (one launch vs the plain kernel looped per query) and the 64-column personalised
+    PageRank adjoint (batched vs looped per teleport vector). Each is the line of its own --workload run
+    with fewer timed steps."""
+    import argparse as _ap
+
+    ea = _ap.Namespace(**vars(args))
+    ea.steps = max(1, min(args.steps, 10))
+    ea.no_cpu_baseline = True
+    ea.scale = SCALE
+    out = {}
+    g = bench_grid(ea, emit=False)
+    out["grid"] = {k: g[k] for k in ("metric", "value", "unit", "ms_per_step", "per_algo", "config")}
+    b = bench_batch(ea, emit=False)
+    out["batch"] = {k: b[k] for k in ("metric", "value", "unit", "ms_per_step", "plain_loop", "speedup_vs_plain_loop",
+                                       "speedup_vs_plain_kernels", "gteps", "parity_with_plain", "config", "energy")}
+    p = bench_ppr(ea, emit=False)
+    out["ppr"] = {k: p[k] for k in ("metric", "value", "unit", "ms_per_step", "sweeps", "plain_loop",
+                                     "speedup_vs_plain_loop", "parity_batched_vs_loop", "roofline", "e2e", "config",
+                                     "energy")}
+    out["extras_steps"] = ea.steps
+    return out
 
 
 def make_batch_inputs(E, num_graphs: int, seed: int = 4):
@@ -414,7 +468,7 @@ def make_batch_inputs(E, num_graphs: int, seed: int = 4):
     return graphs, queries
 
 
-def bench_batch(args) -> None:
+def bench_batch(args, emit: bool = True):
     """Batched queries: one launch (captured CUDA graph) of the work-queue kernel against the plain
     persistent kernel looped per query, on the same GPU; values compared query by query. With N GPUs
     (torchrun) the queries are split by estimated work (graph edges + vertices; eegraph_gb300.shard_queries,
@@ -458,33 +512,38 @@ def bench_batch(args) -> None:
         # plain: the single-query persistent kernel, one call per query, into the same layout
         plain_out = torch.zeros(words, dtype=torch.int32, device="cuda")
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        plain_ms = []
+        plain_ms, plain_kernel_ms = [], []
         reached = 0
         for rep in range(max(1, min(args.steps, 2)) + 1):
             torch.cuda.synchronize()
             ev0.record()
+            kms = 0.0
             for qi, (gi, algo, src) in enumerate(queries):
                 _, r = vgs[gi].run(algo, "sync_push_dd", src, out_device_ptr=plain_out.data_ptr() + 4 * offs[qi],
                                    stream=stream)
+                kms += r["kernel_ms"]  # the query's own kernel time (CUDA events around its launch)
                 if rep == 0:
                     reached += r["reached_edges"]
             ev1.record()
             torch.cuda.synchronize()
             if rep > 0:  # the first pass warms the per-graph workspaces
                 plain_ms.append(ev0.elapsed_time(ev1))
+                plain_kernel_ms.append(kms)
         same = bool(np.array_equal(batched, plain_out.cpu().numpy().view(np.uint32)))
     for g in vgs:
         g.close()
     bms, pms = statistics.median(batch_ms), statistics.median(plain_ms)
+    pkms = statistics.median(plain_kernel_ms)
     # whole job: the slowest GPU's time, the sum of the GPUs' work
     bms, nq = reduce_job(bms, float(len(queries)), world, dev)
     pms, reached = reduce_job(pms, float(reached), world, dev)
+    pkms, _ = reduce_job(pkms, 0.0, world, dev)
     _, n_same = reduce_job(0.0, 1.0 if same else 0.0, world, dev)
     same = n_same == world
     if world > 1:
         torch.distributed.destroy_process_group()
     if rank != 0:
-        return
+        return None
     line = {"metric": f"batched queries/s (BFS/SSSP/SSWP mix over {len(all_graphs)} graphs) vs the plain kernel "
                       "looped per query",
             "value": round(nq / (bms * 1e-3), 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -494,10 +553,16 @@ def bench_batch(args) -> None:
                                    f"K={args.k}, cluster size {cluster} (autotuned)",
                        "graphs": len(all_graphs), "queries": int(nq), "edges": total_edges,
                        "parallelism": f"queries split by estimated work over {world} GPU(s)"},
-            "plain_loop": {"ms_per_step": round(pms, 3), "queries_per_s": round(nq / (pms * 1e-3), 1)},
-            "speedup_vs_plain_loop": round(pms / bms, 2), "gteps": round(reached / (bms * 1e-3) / 1e9, 3),
+            "plain_loop": {"ms_per_step": round(pms, 3), "queries_per_s": round(nq / (pms * 1e-3), 1),
+                           "kernel_ms_per_step": round(pkms, 3),
+                           "note": "ms_per_step: CUDA events around the whole loop (launches and host round trips "
+                                   "included); kernel_ms_per_step: the sum of the queries' own kernel times"},
+            "speedup_vs_plain_loop": round(pms / bms, 2), "speedup_vs_plain_kernels": round(pkms / bms, 2),
+            "gteps": round(reached / (bms * 1e-3) / 1e9, 3),
             "parity_with_plain": same, "clocks": clk.summary(), "energy": energy_line}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 PPR_SCALE, PPR_COLS, PPR_SEEDS = 20, 64, 32
@@ -532,7 +597,7 @@ def ppr_cpu_baseline(budget_s: float, scale: int = 14, cols: int = 64) -> dict:
             "seconds": dt}
 
 
-def bench_ppr(args) -> None:
+def bench_ppr(args, emit: bool = True):
     """Differentiable personalised PageRank: forward + adjoint + gradients for 64 teleport vectors in
     one batched call pair, against the single-column kernels looped per teleport vector. With N GPUs
     (torchrun) the columns are split (eegraph_gb300.shard_columns): each GPU solves its columns on the
@@ -658,13 +723,14 @@ def bench_ppr(args) -> None:
     if dist is not None:
         dist.destroy_process_group()
     if rank != 0:
-        return
+        return None
     fkm = statistics.median(r["kernel_ms"] for r in fwd)
     fby = statistics.median(r["algorithmic_bytes"] for r in fwd)
     fit = int(statistics.median(r["iterations"] for r in fwd))
     ait = int(statistics.median(r["iterations"] for r in adj))
     peak, peak_kind = load_peaks()
     ach = fby / (fkm * 1e-3) / 1e9
+    traffic = load_traffic("k_ppr_rows", f"ppr_s{scale}_k{args.k}") if C > 32 else None
     h2d = 2 * n * C_all * 4                     # all GPUs: their teleport and dLoss/dX columns
     d2h = world * m * 4 + n * C_all * 4         # each GPU reads the summed dLoss/dw and its dLoss/dT columns
     line = {
@@ -685,9 +751,12 @@ def bench_ppr(args) -> None:
         "parity_batched_vs_loop": parity,
         "roofline": {"bound": "hbm", "kernel": "k_ppr_rows (forward solve)", "achieved": round(ach, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4), "peak_source": peak_kind,
-                     "traffic": load_traffic("k_ppr_rows", f"ppr_s{scale}_k{args.k}") if C > 32 else None,
+                     "traffic": traffic,
+                     "dram_achieved": round(traffic / (fkm * 1e-3) / 1e9, 1) if traffic else None,
+                     "dram_frac": round(traffic / (fkm * 1e-3) / 1e9 / peak, 4) if traffic else None,
                      "note": "algorithmic bytes count every row gather as DRAM traffic; at 64 columns about "
-                             "79 % of them hit L2 (traffic = measured DRAM bytes per launch), so frac can exceed 1"},
+                             "79 % of them hit L2 (traffic = measured DRAM bytes per launch), so frac can exceed 1; "
+                             "dram_frac = measured DRAM bytes per launch / kernel time / peak"},
         "e2e": {"value": round(C_all / (e2e_med * 1e-3), 2) if e2e_med else None, "unit": "PR-grad/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(e2e_med, 3) if e2e_med else None},
@@ -703,13 +772,15 @@ def bench_ppr(args) -> None:
                                 "unit": "PR-grad/s", "cores": 1, "kind": "port",
                                 "sample": f"FP64 oracle, R-MAT s14 x 64 columns ({cb['seconds']:.1f} s), "
                                           "scaled by edges x sweeps to the full workload"}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 GRID_SIDE, GRID_SEED = 4096, 7
 
 
-def bench_grid(args) -> None:
+def bench_grid(args, emit: bool = True):
     """High-diameter road-like graph: 4096 x 4096 grid, 4-neighbour undirected, 10 % of edges deleted,
     0.1 % long-range shortcuts, weights U[1,1000], seed 7. BFS/SSSP/SSWP sync_push_dd from vertex 0, one
     persistent launch each, against the same kernels run one launch per round with a host round trip
@@ -721,7 +792,7 @@ def bench_grid(args) -> None:
 
     rank, world, local = dist_env()
     if rank != 0:
-        return
+        return None
     torch.cuda.set_device(local)
     E.lib().eeg_set_device(local)
     side = args.grid_side
@@ -777,7 +848,9 @@ def bench_grid(args) -> None:
                         "covers": "timed persistent runs of the three algorithms"} if energy_ok and joules > 0
                        else {"joules": None, "note": "below the energy counter's resolution over these runs"}
                        if energy_ok else {"unavailable": "NVML energy counter not available"})}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 # ---------------------------------------------------------------- CPU (reference) path
@@ -940,6 +1013,8 @@ def main() -> None:
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline only: skip the grid, batch and personalised-PageRank summaries")
     ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
                     help="subset of the step to run (profiling); the headline uses all five")
     ap.add_argument("--workload", default="rmat", choices=["rmat", "grid", "batch", "ppr"],
