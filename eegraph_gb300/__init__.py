@@ -44,6 +44,7 @@ EXPORTED = [
     "eeg_batch_autotune", "eeg_batch_destroy", "eeg_autotune_k", "eeg_autotune", "eeg_batch_query_times",
     "eeg_ppr_create", "eeg_ppr_set_weights", "eeg_ppr_forward", "eeg_ppr_adjoint", "eeg_ppr_destroy",
     "eeg_batch_set_grid_queries", "eeg_batch_get_config",
+    "eeg_stream_create", "eeg_stream_get_info", "eeg_stream_run", "eeg_stream_destroy",
 ]
 NOALLOC_SCRATCH_BYTES = 32 << 20
 
@@ -68,6 +69,11 @@ class Options(C.Structure):
                 ("timeout_us", C.c_uint32), ("reserved", C.c_uint32 * 3)]
 
 
+class StreamInfo(C.Structure):
+    _fields_ = [("num_nodes", C.c_uint32), ("num_edges", C.c_uint64), ("K", C.c_uint32),
+                ("partition_parts", C.c_uint32), ("device_budget_bytes", C.c_uint64), ("host_bytes", C.c_uint64)]
+
+
 class Tuning(C.Structure):
     _fields_ = [("K", C.c_uint32), ("variant", C.c_int), ("ms", C.c_float), ("ms_table", C.c_float * 12)]
 
@@ -77,7 +83,7 @@ class Result(C.Structure):
                 ("reached_edges", C.c_uint64), ("parts_processed", C.c_uint64), ("edges_scanned", C.c_uint64),
                 ("updates", C.c_uint64), ("algorithmic_bytes", C.c_double), ("gteps", C.c_double),
                 ("pr_residual", C.c_double), ("pr_l1_norm", C.c_double), ("num_activity", C.c_uint32),
-                ("launches", C.c_uint32), ("reserved", C.c_uint32 * 6)]
+                ("launches", C.c_uint32), ("partitions", C.c_uint32), ("reserved", C.c_uint32 * 5)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -145,6 +151,11 @@ def _load() -> C.CDLL:
         "eeg_ppr_adjoint": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.POINTER(Options), vp,
                                       C.POINTER(Result)]),
         "eeg_ppr_destroy": (None, [vp]),
+        "eeg_stream_create": (C.c_int, [vp, C.c_uint32, C.c_uint64, C.POINTER(vp)]),
+        "eeg_stream_get_info": (C.c_int, [vp, C.POINTER(StreamInfo)]),
+        "eeg_stream_run": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint32, C.POINTER(Options), vp, C.c_int, vp,
+                                     C.POINTER(Result)]),
+        "eeg_stream_destroy": (None, [vp]),
         "eeg_energy_begin": (C.c_int, [C.c_int, C.c_char_p, C.c_uint32, C.POINTER(vp)]),
         "eeg_energy_mark": (C.c_int, [vp]),
         "eeg_energy_end": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
@@ -385,6 +396,69 @@ class VirtualGraph:
     def close(self) -> None:
         if self._h:
             _lib.eeg_vgraph_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- graphs larger than device memory
+class StreamGraph:
+    """Active-subgraph streaming (eeg_stream_*): the graph's CSR stays in page-locked host memory and each
+    round's active edges are gathered by the GPU into partition buffers of `budget_bytes` (0 = a quarter of
+    the free device memory). Same results as VirtualGraph.run for BFS, SSSP, SSWP and CC."""
+
+    def __init__(self, graph: Graph, K: int = 8, budget_bytes: int = 0):
+        self.graph = graph
+        h = C.c_void_p()
+        _check(_lib.eeg_stream_create(graph._h, K, budget_bytes, C.byref(h)), "stream_create")
+        self._h = h
+
+    @classmethod
+    def from_arrays(cls, num_nodes: int, src, dst, w=None, K: int = 8, budget_bytes: int = 0) -> "StreamGraph":
+        return cls(Graph.from_arrays(num_nodes, src, dst, w), K, budget_bytes)
+
+    def info(self) -> dict:
+        i = StreamInfo()
+        _check(_lib.eeg_stream_get_info(self._h, C.byref(i)), "stream_info")
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def run(self, algo, variant="sync_push_dd", source: int = 0, *, max_iterations: int = 0,
+            cc_components: bool = False, out_device_ptr: int | None = None, stream: int | None = None,
+            check: bool = True):
+        a = ALGOS[algo] if isinstance(algo, str) else int(algo)
+        v = VARIANTS[variant] if isinstance(variant, str) else int(variant)
+        o = Options()
+        _lib.eeg_options_init(C.byref(o))
+        o.max_iterations = max_iterations
+        o.cc_components = 1 if cc_components else 0
+        n = self.info()["num_nodes"]
+        if out_device_ptr is not None:
+            outp, on_dev, vals = C.c_void_p(out_device_ptr), 1, None
+        else:
+            vals = np.empty(n, np.uint32)
+            outp, on_dev = _ptr(vals), 0
+        r = Result()
+        st = _lib.eeg_stream_run(self._h, a, v, source, C.byref(o), outp, on_dev, C.c_void_p(stream) if stream else None,
+                                 C.byref(r))
+        if check:
+            _check(st, f"stream_run {algo}/{variant}")
+        res = r.as_dict()
+        res["status"] = st
+        return vals, res
+
+    def close(self) -> None:
+        if self._h:
+            _lib.eeg_stream_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):

@@ -29,7 +29,8 @@ NVCC = str(CUDA_HOME / "bin" / "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["builder.cu", "traverse_bfs.cu", "traverse_sssp.cu", "traverse_sswp.cu", "traverse_cc.cu",
-              "traverse_host.cu", "pagerank.cu", "pagerank_dd.cu", "capi.cu", "noalloc.cu", "batch.cu", "ppr.cu"]
+              "traverse_host.cu", "pagerank.cu", "pagerank_dd.cu", "capi.cu", "noalloc.cu", "batch.cu", "ppr.cu",
+              "stream.cu"]
 CPP_SOURCES = ["host_graph.cpp", "energy.cpp"]
 FACADE_SOURCES = ["facade/graph.cpp", "facade/virtual_graph.cpp", "facade/argument_parsing.cpp",
                   "facade/utilities.cpp", "facade/eegraph.cpp"]

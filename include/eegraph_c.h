@@ -244,7 +244,8 @@ typedef struct eeg_result {
     double pr_l1_norm;          /* PageRank: ||x||_1 (FP64) */
     uint32_t num_activity;      /* entries written to activity[] */
     uint32_t launches;          /* kernels this call launched (persistent kernel + set-up/statistics) */
-    uint32_t reserved[6];
+    uint32_t partitions;        /* streamed runs (eeg_stream_run): partitions gathered over all rounds */
+    uint32_t reserved[5];
 } eeg_result;
 
 /* Default options (all zero fields -> defaults). */
@@ -383,6 +384,41 @@ EEG_API eeg_status eeg_ppr_adjoint(eeg_ppr* p, const float* dl_dx, int in_on_dev
                                    float* dl_dw, float* dl_dwn, int out_on_device, int accumulate,
                                    const eeg_options* opts, void* stream, eeg_result* res);
 EEG_API void eeg_ppr_destroy(eeg_ppr* p);
+
+/* ------------------------------------------------------------------ graphs larger than device memory */
+
+/* Active-subgraph streaming, the model of the Subway code vendored in the reference
+ * (Subway/shared/subgraph_generator.cu:10-97 generates each round's active subgraph,
+ * Subway/shared/partitioner.cu:12-91 cuts it into partitions of at most a quarter of device memory,
+ * Subway/subway/{bfs,sssp,sswp,cc}-{sync,async}.cu run the rounds). The graph's CSR stays in
+ * page-locked host memory mapped into the GPU; the device keeps O(num_nodes) state plus two partition
+ * buffers within `device_budget_bytes` (0 = a quarter of the free device memory, as Subway). Each round,
+ * the active vertices' out-edges, in K-bounded parts, are gathered by the GPU straight from host memory
+ * into one buffer while the previous partition is relaxed from the other. Results equal eeg_run's (the
+ * same fixed points) for any budget. A budget below two parts of K targets, K weights and an owner
+ * (2*(8K+4) bytes) is rejected (EEG_ERR_INVALID); graphs of 2^32 or more virtual parts are unsupported. */
+typedef struct eeg_stream eeg_stream;
+typedef struct eeg_stream_info {
+    uint32_t num_nodes;
+    uint64_t num_edges;
+    uint32_t K;
+    uint32_t partition_parts;      /* parts one partition buffer holds */
+    uint64_t device_budget_bytes;  /* bytes of the two partition buffers */
+    uint64_t host_bytes;           /* page-locked host bytes of the CSR */
+} eeg_stream_info;
+/* Build the host CSR from a loaded edge list (1-based files shifted down by one) on the current device. */
+EEG_API eeg_status eeg_stream_create(const eeg_graph* g, uint32_t K, uint64_t device_budget_bytes, eeg_stream** out);
+EEG_API eeg_status eeg_stream_get_info(const eeg_stream* s, eeg_stream_info* out);
+/* BFS, SSSP, SSWP or CC (every vertex seeded; cc_components honoured). SYNC_* variants relax each
+ * partition once per round (Subway's *-sync); ASYNC_* variants also relax a partition again, from HBM,
+ * while its own vertices keep improving (Subway's *-async). max_iterations caps the rounds.
+ * out: num_nodes uint32 values, host memory unless out_on_device != 0. eeg_result: iterations =
+ * rounds, parts_processed = parts streamed, edges_scanned = edges relaxed, partitions = partitions
+ * gathered, kernel_ms = the whole streamed run (gathers included). */
+EEG_API eeg_status eeg_stream_run(eeg_stream* s, eeg_algo algo, eeg_variant variant, uint32_t source,
+                                  const eeg_options* opts, uint32_t* out, int out_on_device, void* stream,
+                                  eeg_result* res);
+EEG_API void eeg_stream_destroy(eeg_stream* s);
 
 /* ------------------------------------------------------------------ energy (NVML) */
 
