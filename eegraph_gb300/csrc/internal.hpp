@@ -79,6 +79,7 @@ struct Workspace {
     uint32_t* dist = nullptr;     // n
     uint32_t* q[2] = {nullptr, nullptr};  // P each
     uint32_t* stamp = nullptr;    // n
+    uint32_t* pushed = nullptr;   // P: the owner value each part last pushed with (DD rounds)
     uint32_t* far = nullptr;      // 4n: three far piles and the far flags (bucketed rounds)
     uint32_t* activity = nullptr; // device copy of the activity vector
     uint32_t activity_cap = 0;

@@ -30,6 +30,7 @@ static eeg_status ensure_traversal_ws(eeg_vgraph* vg, uint32_t activity_cap) {
     const size_t n = vg->n, P = std::max<uint64_t>(vg->fwd.P, 1);
     if (!ws.dist) EEG_TRY(vg_alloc(vg, (void**)&ws.dist, sizeof(uint32_t) * std::max<size_t>(n, 1)));
     if (!ws.stamp) EEG_TRY(vg_alloc(vg, (void**)&ws.stamp, sizeof(uint32_t) * std::max<size_t>(n, 1)));
+    if (!ws.pushed) EEG_TRY(vg_alloc(vg, (void**)&ws.pushed, sizeof(uint32_t) * P));
     if (!ws.q[0]) EEG_TRY(vg_alloc(vg, (void**)&ws.q[0], sizeof(uint32_t) * P));
     if (!ws.q[1]) EEG_TRY(vg_alloc(vg, (void**)&ws.q[1], sizeof(uint32_t) * P));
     if (!ws.tctrl) EEG_CUDA(cudaMalloc((void**)&ws.tctrl, sizeof(TravCtrl)));
@@ -86,6 +87,7 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     a.q0 = ws.q[0];
     a.q1 = ws.q[1];
     a.stamp = ws.stamp;
+    a.pushed = ws.pushed;
     a.ctrl = ws.tctrl;
     a.activity = activity_host ? ws.activity : nullptr;
     a.activity_cap = activity_host ? activity_cap : 0;
