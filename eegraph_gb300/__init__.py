@@ -75,7 +75,8 @@ class StreamInfo(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("K", C.c_uint32), ("variant", C.c_int), ("ms", C.c_float), ("ms_table", C.c_float * 12)]
+    _fields_ = [("K", C.c_uint32), ("variant", C.c_int), ("ms", C.c_float), ("ms_table", C.c_float * 12),
+                ("blocks_per_sm", C.c_uint32), ("ms_per_blocks", C.c_float * 2)]
 
 
 class Result(C.Structure):
@@ -715,7 +716,8 @@ def autotune_k(num_nodes: int, src, dst, w=None, reps: int = 3):
 
 def autotune(num_nodes: int, src, dst, w=None, algo="sssp", reps: int = 3) -> dict:
     """Fastest (K, variant) for this graph and algorithm among K in {4, 8, 16} and the variants with the
-    default's fixed point; returns {"K", "variant", "ms", "table": {(K, variant): ms}}."""
+    default's fixed point, then the number of resident CTAs per SM for it; returns {"K", "variant", "ms",
+    "table": {(K, variant): ms}, "blocks_per_sm", "ms_per_blocks": {b: ms}}."""
     src, dst = _u32(src), _u32(dst)
     wi = _u32(w) if w is not None else None
     a = ALGOS[algo] if isinstance(algo, str) else int(algo)
@@ -723,7 +725,9 @@ def autotune(num_nodes: int, src, dst, w=None, algo="sssp", reps: int = 3) -> di
     _check(_lib.eeg_autotune(num_nodes, src.size, _ptr(src), _ptr(dst), _ptr(wi), a, reps, C.byref(t)), "autotune")
     names = {v: k for k, v in VARIANTS.items()}
     table = {((4, 8, 16)[i // 4], names[i % 4]): t.ms_table[i] for i in range(12) if t.ms_table[i] >= 0}
-    return {"K": t.K, "variant": names[t.variant], "ms": t.ms, "table": table}
+    per_blocks = {b + 1: t.ms_per_blocks[b] for b in range(2) if t.ms_per_blocks[b] >= 0}
+    return {"K": t.K, "variant": names[t.variant], "ms": t.ms, "table": table, "blocks_per_sm": t.blocks_per_sm,
+            "ms_per_blocks": per_blocks}
 
 
 # ---------------------------------------------------------------- energy

@@ -475,6 +475,32 @@ EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const ui
         eeg_vgraph_destroy(vg);
         if (s != EEG_OK) return s;
     }
+    // resident CTAs per SM for the chosen (K, variant)
+    t.blocks_per_sm = 0;
+    t.ms_per_blocks[0] = t.ms_per_blocks[1] = -1.f;
+    {
+        eeg_vgraph* vg = nullptr;
+        EEG_TRY(eeg_vgraph_build_arrays(num_nodes, num_edges, src, dst, w, t.K, flags, nullptr, &vg));
+        const bool pull = algo == EEG_PR && (t.variant == EEG_SYNC_PUSH_TD || t.variant == EEG_ASYNC_PUSH_TD);
+        eeg_status s = EEG_OK;
+        for (uint32_t b = 1; b <= (pull ? 1u : 2u) && s == EEG_OK; ++b) {
+            eeg_options o;
+            eeg_options_init(&o);
+            o.blocks_per_sm = b;
+            std::vector<float> times;
+            for (uint32_t r = 0; r < reps + 1 && s == EEG_OK; ++r) {
+                eeg_result res{};
+                s = eeg_run(vg, algo, t.variant, vg->max_deg_vertex, &o, nullptr, 0, nullptr, 0, nullptr, &res);
+                if (s == EEG_OK && r > 0) times.push_back(res.kernel_ms);
+            }
+            if (s != EEG_OK) break;
+            std::sort(times.begin(), times.end());
+            t.ms_per_blocks[b - 1] = times[times.size() / 2];
+            if (t.blocks_per_sm == 0 || t.ms_per_blocks[b - 1] < t.ms_per_blocks[t.blocks_per_sm - 1]) t.blocks_per_sm = b;
+        }
+        eeg_vgraph_destroy(vg);
+        if (s != EEG_OK) return s;
+    }
     *out = t;
     return EEG_OK;
 }

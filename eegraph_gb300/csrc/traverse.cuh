@@ -208,14 +208,14 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
     // unique). Seeding every vertex (ASYNC_PUSH_DD) makes round 0 dense and in place: a vertex reached in
     // it may push again in the same round, so levels in a queue mix and claims need the stamps.
     const bool bfs_levels = OP == OP_BFS && !TD && !a.seed_all;
-    // Queued parts that already pushed their owner's current value skip their expansion: every target
-    // holds at most that value (+) the weight already (values move one way), and an improvement of the
-    // owner later in the round re-queues it. A vertex claimed in a round is often reached by its own
-    // parts later in that round (the dense all-seeded round 0 of CC above all), and its next-round
-    // rescan is then redundant: edges scanned per reached edge 2.03 -> 1.20 (CC), 1.59 -> 1.21 (SSSP),
-    // 1.65 -> 1.19 (SSWP) on R-MAT s22, CC 1.33 -> 1.22 ms. Source-seeded BFS has no rescans; its kernel
-    // leaves the check out.
-    const bool use_push = OP != OP_BFS && !TD && !BK && a.pushed != nullptr;
+    // CC: a queued part that already pushed its owner's current value skips its expansion: every target
+    // holds at most that value + the weight already (labels only fall), and an improvement of the owner
+    // later in the round re-queues it. In the dense all-seeded round 0 most vertices are improved before
+    // their own parts are reached and push the improved label, so their round-1 rescan is redundant:
+    // edges scanned per reached edge 2.03 -> 1.20 and 1.33 -> 1.22 ms on R-MAT s22 (symmetrised).
+    // SSSP and SSWP rescan less for it too (1.59 -> 1.21, 1.65 -> 1.19) but take the same time, and the
+    // per-part values cost them 15 % more DRAM traffic, so their kernels leave the check out, as does BFS.
+    const bool use_push = OP == OP_CC && !TD && !BK && a.pushed != nullptr;
     constexpr uint32_t PSENT = OP == OP_SSWP ? 0u : 0xFFFFFFFFu;  // no part ever pushes with it
     uint32_t it = a.it_start;
     bool all_done = true;  // false when this launch stops only because of rounds_limit

@@ -318,14 +318,21 @@ EEG_API eeg_status eeg_autotune_k(uint32_t num_nodes, uint64_t num_edges, const 
  * all but SYNC_PUSH_DD, whose source-seeded fixed point differs -- build the graph (PageRank: its
  * transposed graph only), run from the highest-out-degree vertex, one warm-up then `reps` runs, and
  * keep the median kernel time. ms_table[k_index * 4 + variant] (k_index 0, 1, 2 for K = 4, 8, 16) holds
- * the medians, -1 where a variant is not tried. The CTA shape is not a knob: the persistent kernels
- * run the register-limited shape measured best, and hubs are split into K-bounded parts by the builder
- * rather than handed to warps or CTAs by a degree threshold. Host arrays. */
+ * the medians, -1 where a variant is not tried. Then, for the chosen (K, variant), the number of
+ * resident CTAs per SM: 1 or 2 for the traversal kernels (384 or 512 threads each, so 384-1024 threads
+ * per SM) and the data-driven PageRank kernel (512 threads), 1 for the pull PageRank kernel (its
+ * 1024-thread CTA fills an SM); ms_per_blocks[b-1] holds the median at b CTAs per SM (-1 where not
+ * possible) and blocks_per_sm the faster one -- pass it as eeg_options.blocks_per_sm. The threads per
+ * CTA are fixed per kernel by its register budget (measured best), and the split of hub vertices is K
+ * itself: a vertex of more than K out-edges becomes several parts, expanded by as many threads, instead
+ * of being handed to a warp or a CTA past a degree threshold. Host arrays. */
 typedef struct eeg_tuning {
     uint32_t K;
     eeg_variant variant;
     float ms;
     float ms_table[12];
+    uint32_t blocks_per_sm;
+    float ms_per_blocks[2];
 } eeg_tuning;
 EEG_API eeg_status eeg_autotune(uint32_t num_nodes, uint64_t num_edges, const uint32_t* src, const uint32_t* dst,
                                 const uint32_t* weight, eeg_algo algo, uint32_t reps, eeg_tuning* out);

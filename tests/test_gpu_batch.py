@@ -97,6 +97,9 @@ def test_autotune_k_and_variant(gpu, algo):
     assert t["K"] in (4, 8, 16) and t["ms"] > 0
     assert (t["K"], t["variant"]) in t["table"] and all(v > 0 for v in t["table"].values())
     tried_variants = {v for _, v in t["table"]}
+    # resident CTAs per SM for the chosen configuration: 1 and 2 timed (1 only for the pull PageRank)
+    assert t["blocks_per_sm"] in t["ms_per_blocks"] and all(v > 0 for v in t["ms_per_blocks"].values())
+    assert set(t["ms_per_blocks"]) == ({1} if algo == "pr" and t["variant"].endswith("_td") else {1, 2})
     if algo == "cc":
         assert "sync_push_dd" not in tried_variants and len(t["table"]) == 9
     else:
@@ -109,7 +112,7 @@ def test_autotune_k_and_variant(gpu, algo):
         assert np.abs(x / x.sum() - xr / xr.sum()).sum() <= 1e-6
     else:
         with E.VirtualGraph.build(n, s, d, w, K=t["K"]) as vg:
-            got, _ = vg.run(algo, t["variant"], src)
+            got, _ = vg.run(algo, t["variant"], src, blocks_per_sm=t["blocks_per_sm"])
         assert np.array_equal(got, oracle.expected(algo, t["variant"], n, s, d, w, src))
 
 
