@@ -18,7 +18,9 @@ The default (one GPU) line also carries `grid`, `batch` and `ppr`: the lines of 
 (--workload grid|batch|ppr) measured after the headline with fewer timed steps -- the 4096^2 road-like
 grid against one launch per round, the 256-graph query batch against the plain kernel looped per query
 (its wall time and the sum of its kernel times), the 64-column personalised-PageRank adjoint against the
-single-column kernels looped per teleport vector. --no-extras leaves them out.
+single-column kernels looped per teleport vector -- and `stream`: BFS/SSSP/SSWP on the headline graph held in
+host memory and streamed through device buffers of a quarter of its parts (eeg_stream_*). --no-extras
+leaves them out.
 
 cpu_baseline: the reference's CPU path on one core over the same graph (its seq_cpu sweeps, by the
 oracle's C restatement; PageRank: FP64 oracle sweeps, the reference has none); its outputs also check
@@ -445,8 +447,41 @@ def extras(args) -> dict:
     out["ppr"] = {k: p[k] for k in ("metric", "value", "unit", "ms_per_step", "sweeps", "plain_loop",
                                      "speedup_vs_plain_loop", "parity_batched_vs_loop", "roofline", "e2e", "config",
                                      "energy")}
+    out["stream"] = bench_stream(ea)
     out["extras_steps"] = ea.steps
     return out
+
+
+def bench_stream(args) -> dict:
+    """Active-subgraph streaming (eeg_stream_*) on the headline's R-MAT s22 graph held in host memory,
+    with partition buffers of a quarter of the graph's parts: BFS/SSSP/SSWP sync from the max-degree
+    vertex, checked equal to the in-memory kernels; GTEPS = reached edges / the whole streamed run
+    (gathers over the CPU-GPU link included)."""
+    import eegraph_gb300 as E
+
+    n, (s, d, w), _ = make_inputs(E, args.scale)
+    K = args.k
+    parts = int(np.ceil(np.bincount(s, minlength=n) / K).sum())
+    budget = 2 * (8 * K + 4) * (parts // 4)
+    src = int(np.bincount(s, minlength=n).argmax())
+    per = {}
+    with E.VirtualGraph.build(n, s, d, w, K=K) as vg, E.StreamGraph.from_arrays(n, s, d, w, K=K,
+                                                                               budget_bytes=budget) as sg:
+        for algo in ("bfs", "sssp", "sswp"):
+            want, ref = vg.run(algo, "sync_push_dd", src)
+            sg.run(algo, "sync_push_dd", src)
+            runs = [sg.run(algo, "sync_push_dd", src) for _ in range(max(1, min(args.steps, 3)))]
+            ms = statistics.median(r["kernel_ms"] for _, r in runs)
+            got, r = runs[-1]
+            per[algo] = {"ms": round(ms, 3), "rounds": r["iterations"], "partitions": r["partitions"],
+                         "gteps": round(r["reached_edges"] / (ms * 1e-3) / 1e9, 3),
+                         "in_memory_ms": round(ref["kernel_ms"], 3), "equal_to_in_memory": bool(np.array_equal(got, want)),
+                         "edge_bytes_streamed_GB": round(8 * r["edges_scanned"] / 1e9, 3)}
+        info = sg.info()
+    return {"metric": "GTEPS of streamed runs (graph in host memory, device buffers of a quarter of its parts)",
+            "config": {"workload": f"R-MAT s{args.scale} ef{EF} from the max-out-degree vertex, sync, K={K}",
+                       "device_budget_bytes": info["device_budget_bytes"], "host_bytes": info["host_bytes"]},
+            "per_algo": per}
 
 
 def make_batch_inputs(E, num_graphs: int, seed: int = 4):

@@ -114,6 +114,8 @@ bool ArgumentParser::parse_impl(std::string* error) {
             delta = (unsigned)atoi(v);
         } else if (!strcmp(k, "--cc-components")) {
             ccComponents = is_true(v);
+        } else if (!strcmp(k, "--stream-budget")) {
+            streamBudgetMiB = strtoull(v, nullptr, 10);
         } else {
             *error = std::string("\nThere was an error parsing command line argument <") + k + ">\n" +
                      GenerateHelpString();
@@ -153,6 +155,8 @@ std::string ArgumentParser::GenerateHelpString() {
     str += "\n    [--blocks-per-sm]: cap on resident CTAs per SM for the persistent kernels";
     str += "\n    [--delta]: SSSP/SSWP sync-push-dd bucketed rounds of this key width (Default: 0 = plain)";
     str += "\n    [--cc-components]: CC as connected components, relaxing with weight 0 (Default: false)";
+    str += "\n    [--stream-budget]: MiB of device buffers; > 0 keeps the graph in host memory and streams each "
+           "round's active subgraph (BFS/SSSP/SSWP/CC; Default: 0 = graph on the device)";
     str += "\n\n";
     return str;
 }

@@ -130,15 +130,26 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     Timer totalTimer;
     totalTimer.Start();
     if (en) eeg_energy_mark(en);
+    // --stream-budget: the graph stays in host memory and each round's active subgraph is streamed
+    eeg_stream* sg = nullptr;
+    if (args.streamBudgetMiB > 0) {
+        if (algo == EEG_PR) throw std::invalid_argument("--stream-budget: PageRank is not streamed");
+        eeg_graph* hg = nullptr;
+        check(eeg_graph_from_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), &hg), "host graph");
+        const eeg_status cs = eeg_stream_create(hg, args.partSize, args.streamBudgetMiB << 20, &sg);
+        eeg_graph_destroy(hg);
+        check(cs, "streamed graph");
+    }
     // PageRank's topology-driven pull reads only the transposed graph and the out-degrees; its data-driven
     // variants push along out-edges, so they get the forward parts as well
     const bool pr_dd = algo == EEG_PR && (args.variant == SYNC_PUSH_DD || args.variant == ASYNC_PUSH_DD);
     uint32_t flags = (algo == EEG_PR ? (uint32_t)(pr_dd ? EEG_VG_REVERSE : EEG_VG_REVERSE_ONLY) : 0u) |
                      (um ? (uint32_t)EEG_VG_MANAGED : 0u);
     eeg_vgraph* vg = nullptr;
-    check(eeg_vgraph_build_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), args.partSize, flags,
-                                  nullptr, &vg),
-          "virtual graph build");
+    if (!sg)
+        check(eeg_vgraph_build_arrays(n, graph.num_edges, ea.s.data(), ea.d.data(), ea.w.data(), args.partSize, flags,
+                                      nullptr, &vg),
+              "virtual graph build");
 
     eeg_options o;
     eeg_options_init(&o);
@@ -158,13 +169,20 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
     Timer timer;
     timer.Start();
     if (en) eeg_energy_mark(en);
-    eeg_status s = eeg_run(vg, algo, (eeg_variant)args.variant, (uint32_t)args.sourceNode, &o,
-                           algo == EEG_PR ? (void*)rank.data() : (void*)dist.data(), 0,
-                           args.nodeActivity ? activity.data() : nullptr, (uint32_t)activity.size(), nullptr, &r);
+    eeg_status s;
+    if (sg) {
+        s = eeg_stream_run(sg, algo, (eeg_variant)args.variant, (uint32_t)args.sourceNode, &o, dist.data(), 0, nullptr,
+                           &r);
+    } else {
+        s = eeg_run(vg, algo, (eeg_variant)args.variant, (uint32_t)args.sourceNode, &o,
+                    algo == EEG_PR ? (void*)rank.data() : (void*)dist.data(), 0,
+                    args.nodeActivity ? activity.data() : nullptr, (uint32_t)activity.size(), nullptr, &r);
+    }
     if (en) eeg_energy_mark(en);
     const float runtime = timer.Finish();
     const float total = totalTimer.Finish();
-    eeg_vgraph_destroy(vg);
+    if (vg) eeg_vgraph_destroy(vg);
+    if (sg) eeg_stream_destroy(sg);
     if (s != EEG_OK) {
         if (en) eeg_energy_destroy(en);
         check(s, "run");
@@ -202,7 +220,8 @@ Result run_algo(ArgumentParser& args, G& graph, eeg_algo algo, bool um) {
         if (algo == EEG_PR) {
             utilities::PrintResults(rank.data(), std::min<uint>(30, n));
         } else {
-            const bool seed_all = !(args.variant == SYNC_PUSH_DD) || algo != EEG_CC;
+            // CC seeds every vertex, except SYNC_PUSH_DD on the device graph (src/eegraph.cu:548-553)
+            const bool seed_all = args.streamBudgetMiB > 0 || !(args.variant == SYNC_PUSH_DD) || algo != EEG_CC;
             std::vector<uint> cpu = host_check(algo, algo == EEG_CC ? seed_all : false, n, ea.s, ea.d, ea.w,
                                                (uint)args.sourceNode);
             utilities::PrintResults(cpu.data(), std::min<uint>(30, n));

@@ -198,8 +198,10 @@ class UMVirtualGraph {
 // Command line: the reference's flags (--input --output --efile --estats --source --device --iteration
 // --debug --activity --variant --energy --um --accuracy) with the same defaults and the same
 // behaviour on errors (help text, exit(0)), plus --k {4,8,16}, --tolerance (PageRank L1 bound),
-// --timeout (ms, device waits), --blocks-per-sm, --delta (bucketed SSSP/SSWP rounds) and
-// --cc-components (CC as connected components).
+// --timeout (ms, device waits), --blocks-per-sm, --delta (bucketed SSSP/SSWP rounds),
+// --cc-components (CC as connected components) and --stream-budget (MiB: keep the graph in host memory
+// and stream each round's active subgraph through device buffers of that size, Subway's model;
+// BFS/SSSP/SSWP/CC).
 class ArgumentParser {
    public:
     int argc;
@@ -234,6 +236,7 @@ class ArgumentParser {
     unsigned int blocksPerSM = 0;
     unsigned int delta = 0;        // eeg_options.delta
     bool ccComponents = false;     // eeg_options.cc_components
+    unsigned long long streamBudgetMiB = 0;  // > 0: eeg_stream_* with this device budget
 
     ArgumentParser(int argc, char** argv, bool canHaveSource, bool canHaveItrs);
     bool Parse();

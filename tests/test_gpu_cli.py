@@ -88,6 +88,22 @@ def test_cli_binary_csr_input(graph, tmp_path, weighted):
             assert np.array_equal(got, want), (exe, variant)
 
 
+@pytest.mark.parametrize("exe,algo", [("bfs-main", "bfs"), ("sssp-main", "sssp"), ("cc-main", "cc")])
+def test_cli_stream_budget(graph, tmp_path, exe, algo):
+    """--stream-budget keeps the graph in host memory and streams each round's active subgraph through
+    1 MiB of device buffers (Subway's model): the same output as the device-resident run."""
+    p, n, s, d, w = graph
+    src = int(np.bincount(s, minlength=n).argmax())
+    out = tmp_path / "out.txt"
+    stdout = _run(exe, "--input", p, "--source", src, "--variant", "sync_push_dd", "--output", out,
+                  "--stream-budget", 1, "--debug", "true")
+    assert re.search(r"Processing finished in [\d.]+ \(ms\)\.", stdout)
+    assert "Arrays begin to differ" not in stdout
+    got = _read_out(out, np.uint64)
+    want = oracle.cc_labels(n, s, d, w) if algo == "cc" else oracle.expected(algo, "sync_push_dd", n, s, d, w, src)
+    assert np.array_equal(got, want.astype(np.uint64))
+
+
 def test_cli_pagerank_um_activity_energy(graph, tmp_path):
     p, n, s, d, w = graph
     out, ef, es = tmp_path / "pr.txt", tmp_path / "energy.csv", tmp_path / "stats.csv"
