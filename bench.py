@@ -478,7 +478,10 @@ def bench_stream(args) -> dict:
                          "in_memory_ms": round(ref["kernel_ms"], 3), "equal_to_in_memory": bool(np.array_equal(got, want)),
                          "edge_bytes_streamed_GB": round(8 * r["edges_scanned"] / 1e9, 3)}
         info = sg.info()
+    tot_ms = sum(v["ms"] for v in per.values())
+    tot_edges = sum(v["gteps"] * v["ms"] * 1e6 for v in per.values())
     return {"metric": "GTEPS of streamed runs (graph in host memory, device buffers of a quarter of its parts)",
+            "value": round(tot_edges / (tot_ms * 1e-3) / 1e9, 3), "unit": "GTEPS", "ms_per_step": round(tot_ms, 3),
             "config": {"workload": f"R-MAT s{args.scale} ef{EF} from the max-out-degree vertex, sync, K={K}",
                        "device_budget_bytes": info["device_budget_bytes"], "host_bytes": info["host_bytes"]},
             "per_algo": per}
@@ -1048,14 +1051,18 @@ def main() -> None:
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
+    ap.add_argument("--pr-variant", default="sync_push_td", choices=["sync_push_td", "async_push_td", "sync_push_dd",
+                                                                     "async_push_dd"],
+                    help="PageRank variant of the step (profiling; the headline uses sync_push_td)")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline only: skip the grid, batch and personalised-PageRank summaries")
     ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
                     help="subset of the step to run (profiling); the headline uses all five")
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "grid", "batch", "ppr"],
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "grid", "batch", "ppr", "stream"],
                     help="rmat: the headline (R-MAT s22, five algorithms); grid: the 4096^2 high-diameter graph; "
                          "batch: 256-graph query mixture, batched vs looped; "
-                         "ppr: personalised PageRank forward + adjoint, 64 teleport vectors, batched vs looped")
+                         "ppr: personalised PageRank forward + adjoint, 64 teleport vectors, batched vs looped; "
+                         "stream: the R-MAT graph in host memory, streamed through device buffers")
     ap.add_argument("--batch-graphs", type=int, default=256)
     ap.add_argument("--ppr-columns", type=int, default=PPR_COLS, help="teleport vectors of the ppr workload (1-64)")
     ap.add_argument("--grid-side", type=int, default=GRID_SIDE)
@@ -1063,7 +1070,7 @@ def main() -> None:
     ap.add_argument("--grid-delta-sswp", type=int, default=16, help="SSWP bucket width on the grid (0 = plain)")
     args = ap.parse_args()
     global ALGO_PLAN
-    ALGO_PLAN = [p for p in ALGO_PLAN if p[0] in args.algos.split(",")]
+    ALGO_PLAN = [(a, args.pr_variant if a == "pr" else v) for a, v in ALGO_PLAN if a in args.algos.split(",")]
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":
@@ -1074,6 +1081,17 @@ def main() -> None:
         bench_batch(args)
     elif args.workload == "ppr":
         bench_ppr(args)
+    elif args.workload == "stream":
+        import torch
+
+        import eegraph_gb300 as E
+
+        torch.cuda.set_device(dist_env()[2])
+        E.lib().eeg_set_device(dist_env()[2])
+        line = bench_stream(args)
+        line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                     "data": "synthetic (seeded R-MAT, generated in-process)"})
+        print(json.dumps(line))
     else:
         bench_gpu(args)
 

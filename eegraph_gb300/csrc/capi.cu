@@ -113,7 +113,6 @@ static void free_ws(eeg_vgraph* vg) {
     vg_free(vg, w.dd_r);
     vg_free(vg, w.dd_x);
     vg_free(vg, w.dd_amt);
-    vg_free(vg, w.dd_vq);
     vg_free(vg, w.dd_pq);
     if (w.ddctrl) cudaFree(w.ddctrl);
     if (w.stats) cudaFree(w.stats);

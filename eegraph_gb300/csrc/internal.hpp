@@ -63,7 +63,6 @@ struct PRCtrl {
 // Control block of the data-driven PageRank kernel (residual frontier).
 struct PRDDCtrl {
     BarrierWords bw;
-    uint32_t vlen[3];    // vertex-frontier lengths per round (rotating)
     uint32_t plen[3];    // part-queue lengths per round (rotating)
     uint32_t iterations;
     uint32_t pad;
@@ -97,7 +96,6 @@ struct Workspace {
     double* dd_r = nullptr;       // n: residuals
     double* dd_x = nullptr;       // n: values (FP64 accumulation; the output is written to x)
     double* dd_amt = nullptr;     // n: push amount of each vertex activated in the current round
-    uint32_t* dd_vq = nullptr;    // 2n: vertex frontiers (double-buffered)
     uint32_t* dd_pq = nullptr;    // P: part queue of the current round
     PRDDCtrl* ddctrl = nullptr;
     // misc

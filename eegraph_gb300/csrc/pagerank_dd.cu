@@ -11,17 +11,18 @@
 //
 // GB300 form: one cooperative persistent launch; each round has two phases separated by the bounded
 // grid barrier.
-//   A (vertices): each vertex of the frontier takes its residual t (no push lands in this phase, so a
-//     plain read and reset is exact); if t > acc it adds t to its FP64 value, records its push amount
-//     d * t / outdeg, and its parts join the round's part queue (one reservation per warp; the whole
-//     warp writes a hub's part ids).
-//   B (parts): each queued part pushes its owner's amount to its <= K targets with FP64 atomicAdd, the
-//     K atomics issued together. A push that lifts a residual from <= acc to > acc appends the target to
-//     the next frontier. After phase A no residual exceeds acc and residuals only grow in phase B, so a
-//     vertex crosses at most once per round: the frontier needs no claim stamps and holds each vertex once.
-// Round 0's frontier is every vertex (every residual starts at 1-d). Residuals and values are FP64 (a
-// hub's residual collects ~10^5 pushes per round; FP32 accumulation would not hold the 1e-6 L1 bound);
-// the output is FP32.
+//   A (vertices): a dense scan of the residuals -- every vertex whose residual t exceeds acc (no push
+//     lands in this phase, so a plain read and reset is exact) adds t to its FP64 value, records its push
+//     amount d * t / outdeg, and its parts join the round's part queue (one reservation per warp; the
+//     whole warp writes a hub's part ids). The scan reads 8 bytes per vertex per round; the vertices it
+//     activates are the ones the reference's labels would hold.
+//   B (parts): each queued part pushes its owner's amount to its <= K targets with FP64 reductions
+//     (atomic adds whose old value nobody waits for). A round that queues no part ends the run: every
+//     residual is then <= acc.
+// Residuals and values are FP64 (a hub's residual collects ~10^5 pushes per round; FP32 accumulation
+// would not hold the 1e-6 L1 bound); the output is FP32. Tracking which pushes lift a residual past acc
+// instead of scanning needs the atomics' old values: 25 % slower on R-MAT s22 (154.6 against 123.4 ms),
+// every returning FP64 atomic a long-scoreboard wait.
 // The reference's two DD kernels differ only in when a vertex's label is cleared (in the kernel that
 // processes it, or by clearLabel after it); with the residual taken once per round in a phase of its
 // own that makes no difference, so SYNC_PUSH_DD and ASYNC_PUSH_DD run these same rounds.
@@ -45,8 +46,6 @@ struct DDArgs {
     double* xv;
     double* amt;
     float* x;
-    uint32_t* vq0;
-    uint32_t* vq1;
     uint32_t* pq;
     PRDDCtrl* ctrl;
     double acc;
@@ -94,7 +93,6 @@ __global__ void __launch_bounds__(DD_TPB, 2) k_pagerank_dd(DDArgs a) {
     const uint32_t gtid = blockIdx.x * DD_TPB + threadIdx.x;
     const uint32_t gthreads = gridDim.x * DD_TPB;
     const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t lanemask_lt = (1u << lane) - 1u;
     const uint32_t gwarp = gtid >> 5, nwarps = gthreads >> 5;
     const uint64_t pol = l2_evict_first_policy();
     uint32_t epoch = 0;
@@ -108,35 +106,18 @@ __global__ void __launch_bounds__(DD_TPB, 2) k_pagerank_dd(DDArgs a) {
     if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
 
     for (;; ++it) {
-        const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u, old = (it + 2u) % 3u;
-        if (threadIdx.x == 0) s_len = it ? ld_relaxed(&ctrl->vlen[cur]) : a.n;
-        __syncthreads();
-        uint32_t nv = s_len;
-        __syncthreads();
-        if (nv == 0u) break;
+        const uint32_t cur = it % 3u, nxt = (it + 1u) % 3u;
         if (it >= a.max_iters) {
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_ITER_CAP);
             break;
         }
-        if (nv > a.n) {  // cannot happen (one crossing per vertex per round); never read past the frontier
-            if (blockIdx.x == 0 && threadIdx.x == 0)
-                atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
-            nv = a.n;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            ctrl->vlen[old] = 0u;  // last read in round it-1; written again in round it+1
-            ctrl->plen[nxt] = 0u;  // last read in round it-2; written in round it+1
-        }
-        const uint32_t* vin = (it & 1u) ? a.vq1 : a.vq0;
-        uint32_t* vout = (it & 1u) ? a.vq0 : a.vq1;
-
-        // ---- phase A: take the residuals of the frontier
-        for (uint32_t b0 = gwarp * 32u; b0 < nv; b0 += nwarps * 32u) {
-            const uint32_t i = b0 + lane;
+        if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->plen[nxt] = 0u;  // last read in round it-2
+        // ---- phase A: every vertex whose residual exceeds acc takes it (a dense scan of the residuals)
+        for (uint32_t b0 = gwarp * 32u; b0 < a.n; b0 += nwarps * 32u) {
+            const uint32_t v = b0 + lane;
             uint32_t s0 = 0, np = 0;
-            if (i < nv) {
-                const uint32_t v = it ? __ldcg(&vin[i]) : i;
+            if (v < a.n) {
                 const double t = __ldcg(&a.r[v]);
                 if (t > a.acc) {
                     a.r[v] = 0.0;
@@ -153,51 +134,31 @@ __global__ void __launch_bounds__(DD_TPB, 2) k_pagerank_dd(DDArgs a) {
             append_parts(s0, np, &ctrl->plen[cur], a.pq, a.P, lane);
         }
         if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
-
-        // ---- phase B: push the amounts along the queued parts
         if (threadIdx.x == 0) s_len = ld_relaxed(&ctrl->plen[cur]);
         __syncthreads();
         uint32_t npq = s_len;
-        if (npq > a.P) {  // cannot happen (each activated vertex appends its parts once)
+        __syncthreads();
+        if (npq == 0u) break;  // nothing pushes: every residual stays <= acc
+        if (npq > a.P) {
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
             npq = a.P;
         }
+        // ---- phase B: push the amounts along the queued parts (reductions: no value comes back)
         for (uint32_t b0 = gwarp * 32u; b0 < npq; b0 += nwarps * 32u) {
             const uint32_t i = b0 + lane;
-            const bool valid = i < npq;
-            uint32_t col[K];
-            double am = 0.0;
-            if (valid) {
+            if (i < npq) {
+                uint32_t col[K];
                 const uint32_t p = __ldcg(&a.pq[i]);
-                am = __ldcg(&a.amt[__ldg(&a.vowner[p])]);
+                const double am = __ldcg(&a.amt[__ldg(&a.vowner[p])]);
                 ld_part<K>(a.vcol + (size_t)p * K, col, pol);
                 ++my_parts;
-            } else {
 #pragma unroll
-                for (int k = 0; k < K; ++k) col[k] = NO_EDGE;
-            }
-            // groups of 8 atomics in flight (their returned residuals fit the register budget)
-            constexpr int G = K < 8 ? K : 8;
-#pragma unroll
-            for (int g = 0; g < K; g += G) {
-                double prev[G];
-#pragma unroll
-                for (int k = 0; k < G; ++k)
-                    prev[k] = col[g + k] != NO_EDGE ? atomicAdd(&a.r[col[g + k]], am) : 1.0e300;
-#pragma unroll
-                for (int k = 0; k < G; ++k) {
-                    const bool crossed = prev[k] <= a.acc && prev[k] + am > a.acc;
-                    my_pushes += col[g + k] != NO_EDGE ? 1ull : 0ull;
-                    const uint32_t m = __ballot_sync(0xffffffffu, crossed);
-                    if (m) {
-                        uint32_t base = 0;
-                        if (lane == 0) base = atomicAdd(&ctrl->vlen[nxt], (uint32_t)__popc(m));
-                        base = __shfl_sync(0xffffffffu, base, 0);
-                        const uint32_t pos = base + (uint32_t)__popc(m & lanemask_lt);
-                        if (crossed && pos < a.n) vout[pos] = col[g + k];
+                for (int k = 0; k < K; ++k)
+                    if (col[k] != NO_EDGE) {
+                        atomicAdd(&a.r[col[k]], am);
+                        ++my_pushes;
                     }
-                }
             }
         }
         if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
@@ -282,7 +243,6 @@ eeg_status run_pagerank_dd(eeg_vgraph* vg, eeg_variant variant, const eeg_option
     if (!ws.dd_r) EEG_TRY(vg_alloc(vg, (void**)&ws.dd_r, sizeof(double) * n));
     if (!ws.dd_x) EEG_TRY(vg_alloc(vg, (void**)&ws.dd_x, sizeof(double) * n));
     if (!ws.dd_amt) EEG_TRY(vg_alloc(vg, (void**)&ws.dd_amt, sizeof(double) * n));
-    if (!ws.dd_vq) EEG_TRY(vg_alloc(vg, (void**)&ws.dd_vq, sizeof(uint32_t) * 2 * n));
     if (!ws.dd_pq) EEG_TRY(vg_alloc(vg, (void**)&ws.dd_pq, sizeof(uint32_t) * P));
     if (!ws.ddctrl) EEG_CUDA(cudaMalloc((void**)&ws.ddctrl, sizeof(PRDDCtrl)));
     if (!ws.ev[0]) {
@@ -303,8 +263,6 @@ eeg_status run_pagerank_dd(eeg_vgraph* vg, eeg_variant variant, const eeg_option
     a.xv = ws.dd_x;
     a.amt = ws.dd_amt;
     a.x = ws.x;
-    a.vq0 = ws.dd_vq;
-    a.vq1 = ws.dd_vq + n;
     a.pq = ws.dd_pq;
     a.ctrl = ws.ddctrl;
     a.damping = damping;
