@@ -53,6 +53,7 @@ SAMPLE_SCALE = 18
 ALGO_PLAN = [("bfs", "sync_push_dd"), ("sssp", "sync_push_dd"), ("sswp", "sync_push_dd"),
              ("cc", "async_push_dd"), ("pr", "sync_push_td")]
 PR_TOL = 1e-7
+BFS_PUSH_ONLY = False  # --bfs-push-only
 
 
 def workload_name(scale: int, K: int, pr_k: int = 16) -> str:
@@ -245,7 +246,7 @@ def run_step(vg, vg_sym, vg_pr, source, outs, stream, results):
     for algo, variant in ALGO_PLAN:
         g = vg_sym if algo == "cc" else (vg_pr if algo == "pr" else vg)
         _, res = g.run(algo, variant, source, out_device_ptr=outs[algo], stream=stream,
-                       pr_tolerance=PR_TOL)
+                       pr_tolerance=PR_TOL, bfs_push_only=BFS_PUSH_ONLY)
         results[algo] = res
 
 
@@ -267,7 +268,8 @@ def bench_gpu(args) -> None:
     m, m_sym = s.size, ss.size
     stream = torch.cuda.current_stream(dev).cuda_stream
 
-    vg = E.VirtualGraph.build(n, s, d, w, K=args.k, stream=stream)
+    # BFS pulls in its large rounds over the transposed parts (SSSP and SSWP push only)
+    vg = E.VirtualGraph.build(n, s, d, w, K=args.k, reverse=not BFS_PUSH_ONLY, stream=stream)
     vg_sym = E.VirtualGraph.build(n, ss, ds, ws, K=args.k, stream=stream)
     # PageRank pulls over the transposed graph: its own part size (unweighted)
     vg_pr = E.VirtualGraph.build(n, s, d, None, K=args.pr_k, reverse=True, stream=stream)
@@ -285,7 +287,7 @@ def bench_gpu(args) -> None:
         run_step(vg, vg_sym, vg_pr, source, outs, stream, results)
     torch.cuda.synchronize()
 
-    per_algo = {a: {"ms": [], "edges": [], "bytes": [], "iters": []} for a, _ in ALGO_PLAN}
+    per_algo = {a: {"ms": [], "edges": [], "bytes": [], "iters": [], "scanned": []} for a, _ in ALGO_PLAN}
     step_ms = []
     launches = 0
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
@@ -307,6 +309,7 @@ def bench_gpu(args) -> None:
                 per_algo[a]["edges"].append(teps_edges(a, r, m, m_sym))
                 per_algo[a]["bytes"].append(r["algorithmic_bytes"])
                 per_algo[a]["iters"].append(r["iterations"])
+                per_algo[a]["scanned"].append(r["edges_scanned"])
                 launches += r["launches"]
         torch.cuda.synchronize()
         clk.stop()
@@ -375,6 +378,7 @@ def bench_gpu(args) -> None:
         ed = statistics.median(per_algo[a]["edges"])
         algo_summary[a] = {"kernel_ms": round(ms, 4), "gteps": round(ed / (ms * 1e-3) / 1e9, 3),
                            "iterations": int(statistics.median(per_algo[a]["iters"])),
+                           "edges_scanned": int(statistics.median(per_algo[a]["scanned"])),
                            "algorithmic_GB": round(by / 1e9, 4),
                            "achieved_GBs": round(by / (ms * 1e-3) / 1e9, 1),
                            "roofline_frac": round(by / (ms * 1e-3) / 1e9 / peak, 4)}
@@ -1054,6 +1058,8 @@ def main() -> None:
     ap.add_argument("--pr-variant", default="sync_push_td", choices=["sync_push_td", "async_push_td", "sync_push_dd",
                                                                      "async_push_dd"],
                     help="PageRank variant of the step (profiling; the headline uses sync_push_td)")
+    ap.add_argument("--bfs-push-only", action="store_true",
+                    help="BFS without pull rounds (the headline graph is then built without transposed parts)")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline only: skip the grid, batch and personalised-PageRank summaries")
     ap.add_argument("--algos", default="bfs,sssp,sswp,cc,pr",
@@ -1069,8 +1075,9 @@ def main() -> None:
     ap.add_argument("--grid-delta-sssp", type=int, default=8000, help="SSSP bucket width on the grid (0 = plain)")
     ap.add_argument("--grid-delta-sswp", type=int, default=16, help="SSWP bucket width on the grid (0 = plain)")
     args = ap.parse_args()
-    global ALGO_PLAN
+    global ALGO_PLAN, BFS_PUSH_ONLY
     ALGO_PLAN = [(a, args.pr_variant if a == "pr" else v) for a, v in ALGO_PLAN if a in args.algos.split(",")]
+    BFS_PUSH_ONLY = args.bfs_push_only
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3
     if args.impl == "reference":

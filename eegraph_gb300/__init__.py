@@ -66,7 +66,7 @@ class Options(C.Structure):
                 ("pr_accuracy", C.c_float), ("block_size", C.c_uint32), ("blocks_per_sm", C.c_uint32),
                 ("record_activity", C.c_uint32), ("timeout_ms", C.c_uint32), ("host_loop", C.c_uint32),
                 ("pr_hot_limit", C.c_uint32), ("delta", C.c_uint32), ("cc_components", C.c_uint32),
-                ("timeout_us", C.c_uint32), ("reserved", C.c_uint32 * 3)]
+                ("timeout_us", C.c_uint32), ("bfs_push_only", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class StreamInfo(C.Structure):
@@ -84,7 +84,8 @@ class Result(C.Structure):
                 ("reached_edges", C.c_uint64), ("parts_processed", C.c_uint64), ("edges_scanned", C.c_uint64),
                 ("updates", C.c_uint64), ("algorithmic_bytes", C.c_double), ("gteps", C.c_double),
                 ("pr_residual", C.c_double), ("pr_l1_norm", C.c_double), ("num_activity", C.c_uint32),
-                ("launches", C.c_uint32), ("partitions", C.c_uint32), ("reserved", C.c_uint32 * 5)]
+                ("launches", C.c_uint32), ("partitions", C.c_uint32), ("pull_rounds", C.c_uint32),
+                ("reserved", C.c_uint32 * 4)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -354,7 +355,8 @@ class VirtualGraph:
             pr_tolerance: float = 0.0, pr_damping: float = 0.0, blocks_per_sm: int = 0, timeout_ms: int = 0,
             activity_cap: int = 0, out: np.ndarray | None = None, out_device_ptr: int | None = None,
             stream: int | None = None, check: bool = True, host_loop: bool = False, pr_hot_limit: int = 0,
-            delta: int = 0, cc_components: bool = False, timeout_us: int = 0, pr_accuracy: float = 0.0):
+            delta: int = 0, cc_components: bool = False, timeout_us: int = 0, pr_accuracy: float = 0.0,
+            bfs_push_only: bool = False):
         """Run one algorithm; returns (values, result-dict[, activity]). host_loop=True runs one launch
         per round with a host round trip in between (the reference's loop shape), for comparison.
         cc_components=True (CC only) relaxes with weight 0: connected components, not the reference's
@@ -375,6 +377,7 @@ class VirtualGraph:
         o.cc_components = 1 if cc_components else 0
         o.timeout_us = timeout_us
         o.pr_accuracy = pr_accuracy
+        o.bfs_push_only = 1 if bfs_push_only else 0
         n = self.info()["num_nodes"]
         if out_device_ptr is not None:
             outp, on_dev, vals = C.c_void_p(out_device_ptr), 1, None

@@ -99,6 +99,7 @@ static void free_ws(eeg_vgraph* vg) {
     vg_free(vg, w.q[1]);
     vg_free(vg, w.stamp);
     vg_free(vg, w.pushed);
+    vg_free(vg, w.plist);
     if (w.activity) cudaFree(w.activity);
     if (w.tctrl) cudaFree(w.tctrl);
     vg_free(vg, w.x);

@@ -45,6 +45,9 @@ struct TravCtrl {
     uint32_t fmin[3];   // smallest key recorded in each pile
     uint32_t fcsel[2];  // per round parity: the pile receiving far claims
     uint32_t tsel[2];   // per round parity: the threshold T
+    // BFS pull rounds: length of the list of vertices each pull round left unreached (rotating)
+    uint32_t lcnt[3];
+    uint32_t pull_rounds;
 };
 
 // Control block of the PageRank kernels.
@@ -79,6 +82,7 @@ struct Workspace {
     uint32_t* q[2] = {nullptr, nullptr};  // P each
     uint32_t* stamp = nullptr;    // n
     uint32_t* pushed = nullptr;   // P: the owner value each part last pushed with (DD rounds)
+    uint32_t* plist = nullptr;    // 2n: BFS pull rounds' lists of vertices left unreached (two alternate)
     uint32_t* far = nullptr;      // 4n: three far piles and the far flags (bucketed rounds)
     uint32_t* activity = nullptr; // device copy of the activity vector
     uint32_t activity_cap = 0;

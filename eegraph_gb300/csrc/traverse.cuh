@@ -52,6 +52,9 @@ struct TravArgs {
     uint32_t* q1;
     uint32_t* stamp;
     uint32_t* pushed;      // P: the owner value each part last pushed with (DD; null = every queued part expands)
+    const uint32_t* rvstart;  // source-seeded BFS: the transposed graph's parts (null = push rounds only)
+    const uint32_t* rvcol;
+    uint32_t* plist;          // 2n: the vertices each pull round left unreached (two lists alternate)
     TravCtrl* ctrl;
     uint32_t* activity;
     uint32_t activity_cap;
@@ -117,6 +120,7 @@ __device__ __forceinline__ uint32_t atomic_improve(uint32_t* p, uint32_t v) {
 }
 
 constexpr int WCAP = 256;  // per-warp append buffer (claimed vertices) before a flush to the queue
+constexpr uint32_t PULL_LANE = 4;  // BFS pull rounds: parts a lane walks alone before the warp takes over
 
 // Warp-cooperative append of the warp's claimed vertices to the next queue: one reservation per flush
 // (atomicAdd of the parts total), then every claimed vertex's part ids are written; a vertex with more
@@ -191,7 +195,7 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
     constexpr int T_TPB = trav_tpb<OP>();
     __shared__ uint32_t s_buf[TD ? 1 : T_TPB / 32][TD ? 1 : WCAP];
     __shared__ uint32_t s_next[2];  // per round (alternating): next of this CTA's 32-entry chunks
-    __shared__ uint32_t s_ctl[5];   // this round's control words, read once per CTA
+    __shared__ uint32_t s_ctl[6];   // this round's control words, read once per CTA
 
     TravCtrl* ctrl = a.ctrl;
     const uint32_t gtid = blockIdx.x * T_TPB + threadIdx.x;
@@ -217,6 +221,21 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
     // per-part values cost them 15 % more DRAM traffic, so their kernels leave the check out, as does BFS.
     const bool use_push = OP == OP_CC && !TD && !BK && a.pushed != nullptr;
     constexpr uint32_t PSENT = OP == OP_SSWP ? 0u : 0xFFFFFFFFu;  // no part ever pushes with it
+    // Direction-optimising BFS (source-seeded, one persistent launch): when the frontier's parts are many
+    // against the parts of the vertices not yet reached (14x), a round pulls instead of pushing -- every
+    // unreached vertex reads the levels of its in-neighbours from the transposed parts, part by part, and
+    // takes level it+1 at the first one found at level it (its forward parts are appended, so a push
+    // round can follow); rounds push again once the frontier holds fewer than n/12 vertices. Every CTA
+    // takes the same decision from the same control words. The first pull round walks every vertex and
+    // lists the ones with in-edges that it left unreached; a later pull round walks the last list only
+    // (a superset of the unreached vertices with in-edges, whatever rounds came between). Same levels;
+    // R-MAT s22 from the hub pulls in its two large rounds, the second over 6.5 % of the vertices.
+    constexpr bool BFSBU = OP == OP_BFS && !TD && !BK;
+    constexpr int PVL = K <= 8 ? 4 : 2;  // vertices per lane in a pull round, their loads issued together
+    const bool can_bu = BFSBU && bfs_levels && a.rvstart != nullptr && a.rounds_limit == 0;
+    uint32_t seen_parts = 0;  // forward parts of the vertices reached so far
+    bool bu = false;          // this round pulls
+    uint32_t pj = 0;          // pull rounds so far
     uint32_t it = a.it_start;
     bool all_done = true;  // false when this launch stops only because of rounds_limit
     if (threadIdx.x == 0) s_next[0] = s_next[1] = 0u;
@@ -238,6 +257,7 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
             ctrl->fcsel[0] = 0u;  // round 0 (the source's parts) sends every claim to pile 0 (T = 0)
             ctrl->tsel[0] = 0u;
         }
+        if (BFSBU && blockIdx.x == 0 && threadIdx.x == 0) ctrl->lcnt[0] = ctrl->lcnt[1] = ctrl->lcnt[2] = 0u;
         if (!TD && !a.seed_all && blockIdx.x == 0) {
             const uint32_t s0 = a.vstart[a.source], s1 = a.vstart[a.source + 1];
             for (uint32_t j = threadIdx.x; j < s1 - s0; j += T_TPB) a.q0[j] = s0 + j;
@@ -260,6 +280,10 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
         // grid: those same-address reads queue at one L2 slice); the CTA takes them from shared memory
         if (threadIdx.x == 0) {
             s_ctl[0] = ld_relaxed(&ctrl->qparts[cur]);
+            if (BFSBU) {
+                s_ctl[5] = ld_relaxed(&ctrl->qverts[cur]);
+                s_ctl[1] = ld_relaxed(&ctrl->lcnt[(pj + 2u) % 3u]);  // the last pull round's list
+            }
             if (BK) {
                 const uint32_t f = ld_relaxed(&ctrl->fcsel[it & 1u]);
                 s_ctl[1] = f;
@@ -281,17 +305,27 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
                 a.activity[it - 1] = TD ? produced : ld_relaxed(&ctrl->qverts[cur]);
             if (produced == 0u && fcount == 0u) break;
         }
+        if (can_bu) {
+            const uint32_t fparts = s_ctl[0], fverts = s_ctl[5];
+            seen_parts += fparts;
+            const uint32_t unreached_parts = a.P - (seen_parts < a.P ? seen_parts : a.P);
+            bu = bu ? (uint64_t)fverts * 12u >= a.n : (it > 0 && (uint64_t)fparts * 14u > unreached_parts);
+        }
         uint32_t len;
         const bool swap = TD && a.partner && (it & 1u);
         if (dense) len = swap ? (a.P + (a.P & 1u)) : a.P;
         else len = s_ctl[0];
+        const bool frontier_empty = !dense && len == 0u;
         if (!dense && len > a.P) {  // cannot happen (one claim per vertex per round); never read past the queue
             if (blockIdx.x == 0 && threadIdx.x == 0)
                 atomicCAS(&ctrl->bw.status, (uint32_t)DEV_OK, (uint32_t)DEV_OVERFLOW);
             len = a.P;
         }
+        // a pull round walks every vertex, or the last pull round's list
+        const uint32_t pcnt = BFSBU ? (pj > 0 && s_ctl[1] < a.n ? s_ctl[1] : a.n) : 0u;
+        if (BFSBU && bu) len = (uint32_t)(((uint64_t)pcnt + 32u * PVL - 1u) / (32u * PVL) * 32u);
         bool far_round = false;
-        if (!dense && len == 0u) {
+        if (frontier_empty) {
             if (!BK || fcount == 0u) break;
             if (fcount > a.n) {  // one entry per flagged vertex; never read past the pile
                 if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -310,6 +344,7 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctrl->qparts[old] = 0u;
             ctrl->qverts[old] = 0u;
+            if (BFSBU && bu) ctrl->lcnt[(pj + 1u) % 3u] = 0u;  // the next pull round's list
             if (BK) {  // what the next round reads; the pile two far rounds back is free again
                 ctrl->fcsel[(it + 1u) & 1u] = fdst;
                 ctrl->tsel[(it + 1u) & 1u] = T;
@@ -355,7 +390,14 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
         if (threadIdx.x == 0) s_next[(it + 1u) & 1u] = 0u;
         const uint32_t items = far_round ? fcount : len;
         const uint32_t nch = (items + 31u) / 32u;
-        const uint32_t my_chunks = nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u;
+        // A pull round's chunks are vertex ranges, and a vertex id's low bits set its degree on R-MAT-like
+        // graphs: with chunk b + i * grid (grid = 304 = 16 * 19) a CTA saw the same low bits in every
+        // chunk, and CTAs took 115 to 360 thousand cycles over the same chunk counts (R-MAT s22). There
+        // the CTA takes chunk i * grid + (b + i) mod grid of each row i instead: every chunk once, every
+        // residue in every CTA.
+        const bool rot = BFSBU && bu;
+        const uint32_t my_chunks = rot ? (nch + gridDim.x - 1u) / gridDim.x
+                                       : (nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u);
 
         // Software-pipelined by one chunk: the next chunk is drawn and its queue entries are loaded
         // before the current chunk is expanded, so the queue load is off each part's dependent chain.
@@ -365,9 +407,16 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
             ci = __shfl_sync(0xffffffffu, ci, 0);
             pn = 0xFFFFFFFFu;
             if (ci < my_chunks) {
-                const uint32_t idx = (blockIdx.x + ci * gridDim.x) * 32u + lane;
+                uint32_t ch = blockIdx.x + ci;
+                if (rot) {
+                    while (ch >= gridDim.x) ch -= gridDim.x;
+                    ch += ci * gridDim.x;
+                } else {
+                    ch = blockIdx.x + ci * gridDim.x;
+                }
+                const uint32_t idx = ch * 32u + lane;
                 if (idx < items) {
-                    pn = far_round ? pile_src[idx] : (dense ? idx : qcur[idx]);
+                    pn = far_round ? pile_src[idx] : ((dense || (BFSBU && bu)) ? idx : qcur[idx]);
                     if (swap) pn ^= 1u;
                 }
             }
@@ -398,6 +447,133 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
                     }
                     if (move) wbuf[wcnt + __popc(mask & lanemask_lt)] = p;
                     wcnt += c;
+                }
+                continue;
+            }
+            if (BFSBU && bu) {  // pull: item p covers PVL vertices, 32 apart; each belongs to this lane alone
+                bool want[PVL], claim[PVL];
+                uint32_t vv[PVL], s0[PVL], np[PVL];
+                const uint64_t vb = (uint64_t)(p >> 5) * (32u * PVL) + (p & 31u);
+                const uint32_t* lrd = a.plist + (size_t)((pj + 1u) & 1u) * a.n;  // the last pull round's list
+#pragma unroll
+                for (int k = 0; k < PVL; ++k) {  // every level and part range first, then every first part
+                    const uint64_t li = vb + 32u * k;
+                    const bool ok = p < items && li < pcnt;
+                    const uint32_t v = ok ? (pj > 0 ? lrd[li] : (uint32_t)li) : 0u;
+                    want[k] = claim[k] = false;
+                    vv[k] = v;
+                    s0[k] = np[k] = 0u;
+                    if (ok) {
+                        const uint32_t dv = a.dist[v];
+                        s0[k] = __ldg(&a.rvstart[v]);
+                        np[k] = __ldg(&a.rvstart[v + 1]) - s0[k];
+                        want[k] = dv == INF && np[k] > 0u;
+                    }
+                }
+                {
+                    uint32_t c[PVL][K];
+#pragma unroll
+                    for (int k = 0; k < PVL; ++k) {
+                        if (want[k]) ld_part<K>(a.rvcol + (size_t)s0[k] * K, c[k], pol);
+                        else
+#pragma unroll
+                            for (int i = 0; i < K; ++i) c[k][i] = NO_EDGE;
+                    }
+#pragma unroll
+                    for (int k = 0; k < PVL; ++k) {
+                        bool found = false;
+#pragma unroll
+                        for (int i = 0; i < K; ++i) {
+                            if (c[k][i] != NO_EDGE) {
+                                found |= a.dist[c[k][i]] == it;
+                                ++my_edges;
+                            }
+                        }
+                        if (want[k]) ++my_parts;
+                        claim[k] = found;
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < PVL; ++k) {
+                    // no parent in the first part: the lane walks the next ones up to PULL_LANE ...
+                    const uint32_t lim = want[k] ? (np[k] < PULL_LANE ? np[k] : PULL_LANE) : 0u;
+                    for (uint32_t j = 1; j < lim && !claim[k]; ++j) {
+                        uint32_t c[K];
+                        ld_part<K>(a.rvcol + (size_t)(s0[k] + j) * K, c, pol);
+                        bool found = false;
+#pragma unroll
+                        for (int i = 0; i < K; ++i) {
+                            if (c[i] != NO_EDGE) {
+                                found |= a.dist[c[i]] == it;
+                                ++my_edges;
+                            }
+                        }
+                        ++my_parts;
+                        claim[k] = found;
+                    }
+                    // ... and the warp walks the rest of a longer one, 32 parts at a time
+                    uint32_t big = __ballot_sync(0xffffffffu, want[k] && !claim[k] && np[k] > PULL_LANE);
+                    while (big) {
+                        const int l = __ffs(big) - 1;
+                        big &= big - 1u;
+                        const uint32_t bs0 = __shfl_sync(0xffffffffu, s0[k], l);
+                        const uint32_t bnp = __shfl_sync(0xffffffffu, np[k], l);
+                        bool any = false;
+                        for (uint32_t j0 = PULL_LANE; j0 < bnp && !any; j0 += 32u) {
+                            const uint32_t j = j0 + lane;
+                            bool found = false;
+                            if (j < bnp) {
+                                uint32_t c[K];
+                                ld_part<K>(a.rvcol + (size_t)(bs0 + j) * K, c, pol);
+#pragma unroll
+                                for (int i = 0; i < K; ++i) {
+                                    if (c[i] != NO_EDGE) {
+                                        found |= a.dist[c[i]] == it;
+                                        ++my_edges;
+                                    }
+                                }
+                                ++my_parts;
+                            }
+                            any = __any_sync(0xffffffffu, found);
+                        }
+                        if ((uint32_t)l == lane) claim[k] = any;
+                    }
+                    if (claim[k]) {
+                        a.dist[vv[k]] = it + 1u;  // no other writer: push and pull rounds never mix
+                        ++my_updates;
+                    }
+                    const uint32_t mask = __ballot_sync(0xffffffffu, claim[k]);
+                    if (mask) {
+                        const uint32_t cn = __popc(mask);
+                        if (wcnt + cn > (uint32_t)WCAP) {
+                            warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
+                            wcnt = 0;
+                        }
+                        if (claim[k]) wbuf[wcnt + __popc(mask & lanemask_lt)] = vv[k];
+                        wcnt += cn;
+                    }
+                }
+                // the vertices left unreached go on this round's list, one reservation per chunk (buffering
+                // them per warp to reserve less often made R-MAT s22's first pull round 12 % slower)
+                uint32_t lm[PVL], tot = 0;
+#pragma unroll
+                for (int k = 0; k < PVL; ++k) {
+                    lm[k] = __ballot_sync(0xffffffffu, want[k] && !claim[k]);
+                    tot += __popc(lm[k]);
+                }
+                if (tot) {
+                    uint32_t lb = 0;
+                    if (lane == 0) lb = atomicAdd(&ctrl->lcnt[pj % 3u], tot);
+                    lb = __shfl_sync(0xffffffffu, lb, 0);
+                    uint32_t* lwr = a.plist + (size_t)(pj & 1u) * a.n;
+#pragma unroll
+                    for (int k = 0; k < PVL; ++k) {
+                        if (want[k] && !claim[k]) {
+                            const uint32_t pos = lb + __popc(lm[k] & lanemask_lt);
+                            if (pos < a.n) lwr[pos] = vv[k];  // one entry per vertex: always below n
+                        }
+                        lb += __popc(lm[k]);
+                    }
                 }
                 continue;
             }
@@ -517,6 +693,7 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
         } else if (wcnt) {
             warp_flush(a, wbuf, wcnt, qnext, nxt, lane);
         }
+        if (BFSBU && bu) ++pj;
         if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
     }
 
@@ -536,6 +713,7 @@ finish:
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctrl->iterations = it;
         ctrl->done = all_done ? 1u : 0u;
+        if (BFSBU) ctrl->pull_rounds = pj;
     }
 }
 

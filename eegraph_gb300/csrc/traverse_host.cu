@@ -88,6 +88,13 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
     a.q1 = ws.q[1];
     a.stamp = ws.stamp;
     a.pushed = ws.pushed;
+    // source-seeded BFS pulls in its large rounds when the transposed parts exist
+    if (op == OP_BFS && variant == EEG_SYNC_PUSH_DD && vg->has_rev && vg->rev.P && !o.bfs_push_only && !bucketed) {
+        if (!ws.plist) EEG_TRY(vg_alloc(vg, (void**)&ws.plist, sizeof(uint32_t) * 2 * (size_t)vg->n));
+        a.rvstart = vg->rev.vstart;
+        a.rvcol = vg->rev.vcol;
+        a.plist = ws.plist;
+    }
     a.ctrl = ws.tctrl;
     a.activity = activity_host ? ws.activity : nullptr;
     a.activity_cap = activity_host ? activity_cap : 0;
@@ -143,6 +150,7 @@ eeg_status run_traversal(eeg_vgraph* vg, int op, eeg_variant variant, uint32_t s
         res->parts_processed = hc.parts_processed;
         res->edges_scanned = hc.edges_scanned;
         res->updates = hc.updates;
+        res->pull_rounds = hc.pull_rounds;
     }
     if (activity_host && activity_cap) {
         const uint32_t cnt = std::min<uint32_t>(hc.iterations, activity_cap);

@@ -227,7 +227,10 @@ typedef struct eeg_options {
     uint32_t timeout_us;      /* bound on any device-side wait in microseconds; when nonzero it replaces
                                  timeout_ms (sub-millisecond limits). A wait that runs out makes every CTA
                                  leave and the call return EEG_ERR_TIMEOUT; the handle stays usable. */
-    uint32_t reserved[3];
+    uint32_t bfs_push_only;   /* BFS (SYNC_PUSH_DD): 1 = push rounds only; 0 = pull (bottom-up) rounds while the
+                                 frontier is large, when the graph has its transposed parts (EEG_VG_REVERSE);
+                                 the same levels either way */
+    uint32_t reserved[2];
 } eeg_options;
 
 typedef struct eeg_result {
@@ -245,7 +248,8 @@ typedef struct eeg_result {
     uint32_t num_activity;      /* entries written to activity[] */
     uint32_t launches;          /* kernels this call launched (persistent kernel + set-up/statistics) */
     uint32_t partitions;        /* streamed runs (eeg_stream_run): partitions gathered over all rounds */
-    uint32_t reserved[5];
+    uint32_t pull_rounds;       /* BFS: rounds that pulled over the transposed parts (the rest pushed) */
+    uint32_t reserved[4];
 } eeg_result;
 
 /* Default options (all zero fields -> defaults). */

@@ -304,3 +304,53 @@ def test_host_loop_mode_equals_persistent(gpu, algo, variant):
         assert ra["iterations"] == rb["iterations"]
     assert rb["launches"] == rb["iterations"] + 2  # one per round, the final check, the statistics kernel
     assert ra["launches"] == 2
+
+
+@pytest.mark.parametrize("K", [4, 8, 16])
+def test_bfs_pull_rounds(gpu, K):
+    """Source-seeded BFS on a graph built with its transposed parts pulls in its large rounds (every
+    unreached vertex looks for a parent at the current level among its in-neighbours) and pushes in the
+    others. Levels bit-exact against the oracle and against push rounds only, from the hub (rounds that
+    pull, the second one over the list of vertices the first one left unreached), from a vertex with
+    one out-edge and from a vertex with no out-edges; far fewer edges read than pushing."""
+    n = 1 << 16
+    s, d, w = gpu.gen_rmat(16, 16, seed=1, wmin=1, wmax=63)
+    deg = np.bincount(s, minlength=n)
+    hub = int(deg.argmax())
+    srcs = [hub, int(np.flatnonzero(deg == 1)[0]), int(np.flatnonzero(deg == 0)[0])]
+    with gpu.VirtualGraph.build(n, s, d, w, K=K, reverse=True) as vg:
+        for src in srcs:
+            want = oracle.bfs(n, s, d, src)
+            got, res = vg.run("bfs", "sync_push_dd", src)
+            push, rp = vg.run("bfs", "sync_push_dd", src, bfs_push_only=True)
+            assert np.array_equal(got, want), (src, int((got != want).sum()))
+            assert np.array_equal(push, want) and rp["pull_rounds"] == 0
+            assert res["iterations"] == rp["iterations"]  # one round per level either way
+            assert res["reached_vertices"] == rp["reached_vertices"]
+            if src == hub:
+                assert res["pull_rounds"] >= 2, res["pull_rounds"]
+                assert res["edges_scanned"] * 3 < rp["edges_scanned"], (res["edges_scanned"], rp["edges_scanned"])
+    with gpu.VirtualGraph.build(n, s, d, w, K=K) as vg:  # no transposed parts: push rounds only
+        got, res = vg.run("bfs", "sync_push_dd", hub)
+        assert np.array_equal(got, oracle.bfs(n, s, d, hub)) and res["pull_rounds"] == 0
+
+
+def test_bfs_pull_rounds_symmetric_and_sparse(gpu):
+    """An undirected graph (its in-edges are its out-edges: the forward parts serve both directions)
+    and a sparse graph whose vertices mostly have no in-edges (edge factor 2)."""
+    n = 1 << 15
+    s, d, w = gpu.gen_rmat(15, 16, seed=5, wmin=1, wmax=63)
+    ss, ds, ws = gpu.symmetrize(s, d, w)
+    hub = int(np.bincount(ss, minlength=n).argmax())
+    with gpu.VirtualGraph.build(n, ss, ds, ws, K=8, symmetric=True) as vg:
+        got, res = vg.run("bfs", "sync_push_dd", hub)
+    assert np.array_equal(got, oracle.bfs(n, ss, ds, hub)) and res["pull_rounds"] >= 1
+    with gpu.VirtualGraph.build(n, s, d, w, K=8, symmetrize=True) as vg:  # symmetrised on the device
+        got, res = vg.run("bfs", "sync_push_dd", hub)
+    assert np.array_equal(got, oracle.bfs(n, ss, ds, hub)) and res["pull_rounds"] >= 1
+    s, d, w = gpu.gen_rmat(15, 2, seed=9, wmin=1, wmax=63)
+    hub = int(np.bincount(s, minlength=n).argmax())
+    with gpu.VirtualGraph.build(n, s, d, w, K=8, reverse=True) as vg:
+        for src in (hub, 0):
+            got, _ = vg.run("bfs", "sync_push_dd", src)
+            assert np.array_equal(got, oracle.bfs(n, s, d, src)), src

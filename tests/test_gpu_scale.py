@@ -1,7 +1,8 @@
 """GPU parity at the sizes the benchmark numbers are quoted on (needs a GB300).
 
 * R-MAT scale 22, edge factor 16 (67,108,864 edges), a/b/c/d .57/.19/.19/.05, seed 1, weights U[1,63],
-  source = highest-out-degree vertex: BFS/SSSP/SSWP in every variant at K = 8, CC on the symmetrised
+  source = highest-out-degree vertex: BFS/SSSP/SSWP in every variant at K = 8 (BFS also with the pull
+  rounds the benchmark's graph takes), CC on the symmetrised
   arc set (134 M arcs) in every variant, PageRank (pull over the transposed graph, K = 16, as the
   benchmark builds it) in every variant; at K = 4 and K = 16 SSSP source-seeded and all-seeded and CC
   all-seeded. Integer results bit-exact against the oracle (BFS, Dijkstra, max-min Dijkstra,
@@ -71,6 +72,16 @@ def test_rmat22_traversals_every_variant(gpu, rmat22):
                 assert np.array_equal(got, want), (algo, variant, _mismatch(got, want))
                 if variant == "sync_push_dd":
                     assert res["reached_vertices"] == int((want != (0 if algo == "sswp" else oracle.INF)).sum())
+
+
+def test_rmat22_bfs_pull_rounds(gpu, rmat22):
+    """The benchmark's BFS graph (transposed parts built): pull rounds, levels bit-exact."""
+    n, (s, d, w), src = rmat22["n"], rmat22["g"], rmat22["src"]
+    with gpu.VirtualGraph.build(n, s, d, w, K=8, reverse=True) as vg:
+        got, res = vg.run("bfs", "sync_push_dd", src)
+    want = rmat22["want"]["bfs"]
+    assert np.array_equal(got, want), _mismatch(got, want)
+    assert res["pull_rounds"] == 2 and res["edges_scanned"] * 4 < res["reached_edges"]
 
 
 def test_rmat22_cc_every_variant(gpu, rmat22):
