@@ -408,6 +408,9 @@ eeg_status configure(eeg_batch* b, uint32_t csize) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    int dev = 0;
+    EEG_CUDA(cudaGetDevice(&dev));
+    EEG_TRY(prefer_l1(k_batch, 2, dev));  // the filter reads' L1 hits, as for the single-graph kernels
     int nclusters = 0;
     EEG_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, k_batch, &cfg));
     if (nclusters <= 0) {

@@ -750,6 +750,10 @@ eeg_status launch_one(const TravArgs& args, int device, uint32_t blocks_per_sm_r
     constexpr bool CAN_BK = !TD && (OP == OP_SSSP || OP == OP_SSWP);
     auto kern = (CAN_BK && args.delta && !args.seed_all) ? k_traverse<OP, K, TD, CAN_BK> : k_traverse<OP, K, TD, false>;
     constexpr int T_TPB = trav_tpb<OP>();
+    // The filter reads of dist[] are L1 hits in part, and L1 is what shared memory leaves: ask for the
+    // smallest carveout that still holds the two CTAs per SM the kernel is built for (R-MAT s22: SSSP
+    // 0.725 -> 0.706 ms, SSWP 0.726 -> 0.709, CC 1.215 -> 1.193 against the driver's default).
+    EEG_TRY(prefer_l1(kern, 2, device));
     int per_sm = 0;
     EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T_TPB, 0));
     if (per_sm <= 0) {
