@@ -7,7 +7,6 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
-#include <algorithm>
 #include <string>
 
 #include "../../include/eegraph_c.h"
@@ -94,22 +93,6 @@ __device__ __forceinline__ void ld_part(const uint32_t* p, uint32_t (&o)[K], uin
 #pragma unroll
         for (int i = 0; i < K; i += 8) ld_stream_u8(p + i, o + i);
     }
-}
-
-// Shared-memory carveout hint for a kernel with static shared memory only: the smallest share of the
-// SM's unified L1/shared storage that holds `ctas` CTAs (each also takes 1 KB the system reserves), so
-// the rest stays L1.
-template <typename F>
-inline eeg_status prefer_l1(F kern, int ctas, int device) {
-    cudaFuncAttributes fa;
-    EEG_CUDA(cudaFuncGetAttributes(&fa, (const void*)kern));
-    int smem_sm = 0;
-    EEG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device));
-    if (smem_sm <= 0) return EEG_OK;
-    const long long need = (long long)ctas * ((long long)fa.sharedSizeBytes + 1024);
-    const int pct = (int)std::min<long long>(100, (need * 100 + smem_sm - 1) / smem_sm);
-    EEG_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
-    return EEG_OK;
 }
 
 // Grid-wide barrier for a cooperative launch. `epoch` is a per-CTA counter kept by the caller.

@@ -4,9 +4,26 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "common.cuh"
+
+// Shared-memory carveout hint for a kernel with static shared memory only: the smallest share of the
+// SM's unified L1/shared storage that holds `ctas` CTAs (each also takes 1 KB the system reserves), so
+// the rest stays L1.
+template <typename F>
+inline eeg_status prefer_l1(F kern, int ctas, int device) {
+    cudaFuncAttributes fa;
+    EEG_CUDA(cudaFuncGetAttributes(&fa, (const void*)kern));
+    int smem_sm = 0;
+    EEG_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, device));
+    if (smem_sm <= 0) return EEG_OK;
+    const long long need = (long long)ctas * ((long long)fa.sharedSizeBytes + 1024);
+    const int pct = (int)std::min<long long>(100, (need * 100 + smem_sm - 1) / smem_sm);
+    EEG_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
+    return EEG_OK;
+}
 
 // Host edge list (the reference's Graph: src/graph.cpp, include/graph.hpp:28-50).
 struct eeg_graph {
