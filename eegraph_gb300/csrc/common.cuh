@@ -38,11 +38,13 @@ eeg_status cuda_fail(cudaError_t e, const char* what, const char* file, int line
     } while (0)
 
 // Control words shared by every persistent kernel (first fields of each control block).
-struct BarrierWords {
+// A line of its own: pollers never share it with the round counters that working CTAs update
+// (R-MAT s22: SSSP 0.706 -> 0.700 ms, CC 1.197 -> 1.188, 4096^2 grid SSSP 27.9 -> 27.5 ms).
+struct alignas(128) BarrierWords {
     uint32_t arrive;  // monotone arrival counter (wrap-safe compare)
     uint32_t abort;   // set when any CTA gave up; everyone leaves at the next barrier
     uint32_t status;  // DevStatus (first error wins)
-    uint32_t pad;
+    uint32_t pad[29];
 };
 
 #ifdef __CUDACC__
@@ -51,6 +53,16 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
+}
+// {p[0], p[1]} in one acquire load (p 8-byte aligned)
+__device__ __forceinline__ uint2 ld_acquire_v2(const uint32_t* p) {
+    uint2 v;
+    asm volatile("ld.acquire.gpu.global.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p) : "memory");
+    return v;
+}
+// release-ordered reduction: the writes this thread has made or observed come before the add
+__device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
     uint32_t v;
@@ -128,6 +140,43 @@ __device__ __forceinline__ bool grid_barrier(BarrierWords* bw, uint32_t& epoch, 
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// The same barrier for grids whose CTAs arrive together (PageRank's balanced sweeps): the arrival
+// itself releases the CTA's writes (ordered before this thread by the __syncthreads), and each spin is
+// one acquire load of the arrivals and the abort word together, so the last arrival is seen one L2
+// round trip sooner (R-MAT s22 PageRank, 93 barriers: 17.35 -> 17.10 ms). Where CTAs finish at
+// different times the faster polling slowed the CTAs still working (SSSP 0.700 -> 0.719 ms), so the
+// traversals keep grid_barrier.
+__device__ __forceinline__ bool grid_barrier_sync(BarrierWords* bw, uint32_t& epoch, uint64_t timeout_ns) {
+    __shared__ uint32_t s_ok2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        epoch += 1;
+        const uint32_t target = epoch * gridDim.x;
+        red_release_add(&bw->arrive, 1u);
+        uint32_t ok = 1;
+        const uint64_t t0 = global_timer_ns();
+        uint32_t spins = 0;
+        while (true) {
+            const uint2 w = ld_acquire_v2(&bw->arrive);  // {arrive, abort}
+            if (w.y) { ok = 0; break; }
+            if ((int32_t)(w.x - target) >= 0) break;
+            __nanosleep(32);
+            if ((++spins & 7u) == 0) {
+                const uint64_t now = global_timer_ns();
+                if (now - t0 > timeout_ns) {
+                    atomicCAS(&bw->status, (uint32_t)DEV_OK, (uint32_t)DEV_TIMEOUT);
+                    atomicExch(&bw->abort, 1u);
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        s_ok2 = ok;
+    }
+    __syncthreads();
+    return s_ok2 != 0;
 }
 
 // Knuth's TwoSum: s + e == a + b exactly (round-to-nearest FP32).

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
     if (threadIdx.x == 0 && s_zero) atomicAdd(&ctrl->zero_in, s_zero);
     uint32_t s = 0;
     unsigned long long my_edges = 0;
-    if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
+    if (!grid_barrier_sync(&ctrl->bw, epoch, a.timeout_ns)) goto finish;
     {
         const double zero_norm = (double)*(volatile unsigned long long*)&ctrl->zero_in * (double)a.base;
         for (;; ++s) {
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(PR_TPB, 1) k_pagerank(PRArgs a) {
                 atomicAdd(&ctrl->resid[slot], rr);
                 atomicAdd(&ctrl->norm[slot], nn);
             }
-            if (!grid_barrier(&ctrl->bw, epoch, a.timeout_ns)) break;
+            if (!grid_barrier_sync(&ctrl->bw, epoch, a.timeout_ns)) break;
             // one thread per CTA reads the sweep's totals (every warp reading the same two words would
             // queue at one L2 slice); the CTA takes them from shared memory
             if (threadIdx.x == 0) {
