@@ -392,9 +392,9 @@ __global__ void __launch_bounds__(trav_tpb<OP>(), 2) k_traverse(TravArgs a) {
         const uint32_t nch = (items + 31u) / 32u;
         // A pull round's chunks are vertex ranges, and a vertex id's low bits set its degree on R-MAT-like
         // graphs: with chunk b + i * grid (grid = 304 = 16 * 19) a CTA saw the same low bits in every
-        // chunk, and CTAs took 115 to 360 thousand cycles over the same chunk counts (R-MAT s22). There
-        // the CTA takes chunk i * grid + (b + i) mod grid of each row i instead: every chunk once, every
-        // residue in every CTA.
+        // chunk, and CTAs took 115 to 360 thousand cycles over the same chunk counts (R-MAT s22). In a
+        // pull round a CTA takes chunk i * grid + (b + i) mod grid of each row i instead: every chunk
+        // once, every residue in every CTA.
         const bool rot = BFSBU && bu;
         const uint32_t my_chunks = rot ? (nch + gridDim.x - 1u) / gridDim.x
                                        : (nch > blockIdx.x ? (nch - blockIdx.x + gridDim.x - 1u) / gridDim.x : 0u);
@@ -752,7 +752,7 @@ eeg_status launch_one(const TravArgs& args, int device, uint32_t blocks_per_sm_r
     constexpr int T_TPB = trav_tpb<OP>();
     // The filter reads of dist[] are L1 hits in part, and L1 is what shared memory leaves: ask for the
     // smallest carveout that still holds the two CTAs per SM the kernel is built for (R-MAT s22: SSSP
-    // 0.725 -> 0.706 ms, SSWP 0.726 -> 0.709, CC 1.215 -> 1.193 against the driver's default).
+    // 0.725 -> 0.706 ms, SSWP 0.726 -> 0.709, CC 1.215 -> 1.193 against the CUDA driver's default).
     EEG_TRY(prefer_l1(kern, 2, device));
     int per_sm = 0;
     EEG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T_TPB, 0));
