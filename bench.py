@@ -85,11 +85,17 @@ KERNEL_SOURCES = {"k_traverse": ["traverse.cuh", "traverse_host.cu", "common.cuh
 
 
 def kernel_source_sha(kernel: str) -> str:
+    """Hash of the kernel's source files with comments and blank lines left out (a comment edit keeps
+    a measured figure valid; any code change retires it)."""
     import hashlib
+    import re
 
     h = hashlib.sha1()
     for f in KERNEL_SOURCES[kernel.split("<")[0]]:
-        h.update((ROOT / "eegraph_gb300" / "csrc" / f).read_bytes())
+        text = (ROOT / "eegraph_gb300" / "csrc" / f).read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        h.update("\n".join(ln.rstrip() for ln in text.splitlines() if ln.strip()).encode())
     return h.hexdigest()[:16]
 
 

@@ -93,3 +93,29 @@ def test_clock_sampler_keeps_the_timed_window():
     assert c.summary()["samples"] == 1 and c.summary()["window"] == "whole run"
     c.lines = []
     assert c.summary()["reasons"] == ["unavailable"]
+
+
+def test_traffic_figures_follow_the_kernel_code_not_its_comments(tmp_path, monkeypatch):
+    """A measured DRAM figure (profiles/traffic.json) stays in use across a comment edit of the kernel's
+    sources and is retired by any code change; every committed figure matches the sources here."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    t = json.loads((ROOT / "profiles" / "traffic.json").read_text())
+    for wl, d in t.items():
+        if isinstance(d, dict):
+            for k, e in d.items():
+                if isinstance(e, dict):
+                    assert bench.load_traffic(k, wl) == float(e["dram_bytes_per_launch"]), (wl, k)
+    csrc = tmp_path / "eegraph_gb300" / "csrc"
+    csrc.mkdir(parents=True)
+    for f in bench.KERNEL_SOURCES["k_traverse"]:
+        (csrc / f).write_text((ROOT / "eegraph_gb300" / "csrc" / f).read_text())
+    monkeypatch.setattr(bench, "ROOT", tmp_path)
+    base = bench.kernel_source_sha("k_traverse<OP_BFS>")
+    assert base == t["s22_k8"]["k_traverse<OP_BFS>"]["source_sha"]
+    p = csrc / "traverse.cuh"
+    p.write_text(p.read_text() + "\n// a note\n/* another\n   note */\n\n")
+    assert bench.kernel_source_sha("k_traverse<OP_BFS>") == base
+    p.write_text(p.read_text().replace("constexpr int WCAP = 256;", "constexpr int WCAP = 128;"))
+    assert bench.kernel_source_sha("k_traverse<OP_BFS>") != base
