@@ -393,6 +393,10 @@ def bench_gpu(args) -> None:
     for a in algo_summary:  # measured DRAM bytes per launch (profiles/traffic.json), where captured
         tr = load_traffic(kern_names[a], f"s{scale}_k{args.pr_k if a == 'pr' else args.k}")
         algo_summary[a]["dram_GB_per_launch"] = round(tr / 1e9, 3) if tr else None
+        # the measured DRAM bytes over this run's kernel time: what the kernel moves, where roofline_frac
+        # counts the work-minimal bytes of the reference's push algorithm (BFS's pull rounds skip most)
+        ms = algo_summary[a]["kernel_ms"]
+        algo_summary[a]["dram_frac"] = round(tr / (ms * 1e-3) / 1e9 / peak, 4) if tr else None
     dom = max(algo_summary, key=lambda a: algo_summary[a]["kernel_ms"])
     kern_name = kern_names[dom]
     ach = algo_summary[dom]["achieved_GBs"]
